@@ -1,0 +1,364 @@
+"""Benchmark: pairwise composition-vector distances per second on GB300.
+
+One step = the whole hot path over one batch: build the composition vectors of
+every proteome (K-mer counting, Markov alpha, normalisation) from the residue
+bytes, index them, and compute C (hence D = (1 - C) / 2) for every pair.
+
+  value   device-resident: the residue bytes are in HBM when a step starts;
+          CUDA events on the launching stream around each step; L2 flushed
+          (512 MB write) between steps, outside the timed events.
+  e2e     through the public batched API with host buffers: pinned host bytes
+          -> H2D -> build -> pairs -> D2H of the C matrix, wall clock per step.
+  roofline  the pair kernel (k_allpairs): algorithmic bytes 8 * (nnz_i + nnz_j)
+          per pair over its event-timed duration, against the measured HBM copy
+          bandwidth; values above 1 come from reuse of resident vectors (shared
+          memory tiles and L2), not from DRAM traffic.
+  cpu_baseline  the reference's CPU path (CompositionVectorKernels.buildCPU /
+          compareCPU, restated in C under oracle/) on a bounded sample,
+          OpenMP over proteomes and over pairs, extrapolated to the workload.
+
+``--impl reference`` prints the reference arm: that CPU path, timed the same
+way, as the line's value.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "uniform256"
+WORKLOAD_TEXT = ("uniform256: 256 synthetic proteomes x 1,500 proteins (lognormal lengths, "
+                 "median 300 aa), seed 1, branch substitution rate U(0.01, 0.2), K=6 protein, "
+                 "all 32,640 pairs i<j (+ the 256 self products)")
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_launch():
+    """DRAM bytes of one pair-kernel launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "allpairs_uniform256_dram.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _barrier_max(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline (the reference's CPU path, restated in C under oracle/)
+# ----------------------------------------------------------------------------
+
+def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed=0):
+    from oracle import oracle as O
+    O.lib()
+    threads = threads or O.max_threads()
+    rng = np.random.default_rng(seed)
+    nb = min(len(wl), max(threads, 4))
+    ids = rng.choice(len(wl), nb, replace=False)
+    t0 = time.perf_counter()
+    vecs = O.java_build_many([wl.get(int(i)) for i in ids], 6, threads=threads)
+    t_build = time.perf_counter() - t0
+    build_rate = nb / t_build                                      # proteomes / s
+    pairs = [(a, b) for a in range(nb) for b in range(a + 1, nb)]
+    budget = max(1.0, seconds - t_build)
+    done, t_cmp = 0, 0.0
+    while t_cmp < budget and done < 100000:
+        chunk = pairs * max(1, (4 * threads) // max(len(pairs), 1))
+        t0 = time.perf_counter()
+        O.java_compare_pairs(vecs, chunk, threads=threads)
+        t_cmp += time.perf_counter() - t0
+        done += len(chunk)
+    pair_rate = done / t_cmp                                        # pairs / s
+    total = n_build_total / build_rate + n_pairs_total / pair_rate
+    return {
+        "value": n_pairs_total / total, "unit": "pairs/s", "cores": threads, "kind": "port",
+        "sample": (f"buildCPU of {nb} proteomes ({t_build:.1f} s) + compareCPU of {done} pairs "
+                   f"({t_cmp:.1f} s), OpenMP {threads} threads; extrapolated to "
+                   f"{n_build_total} builds + {n_pairs_total} pairs"),
+        "build_per_s": build_rate, "pairs_per_s_compare_only": pair_rate,
+    }
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return 0
+    from rocket_gb300 import synth
+    wl = synth.workload(WORKLOAD)
+    n = len(wl)
+    n_pairs = n * (n - 1) // 2
+    vals = []
+    base = None
+    for s in range(args.warmup + args.steps):
+        r = cpu_baseline(wl, n_pairs, n, seconds=args.ref_seconds, seed=s)
+        if s >= args.warmup:
+            vals.append(r["value"])
+            base = r
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": "pairwise CV distances/s", "value": value,
+        "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * n_pairs / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 (java float path)", "data": "synthetic",
+        "config": {"workload": WORKLOAD_TEXT},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": base["cores"],
+                         "kind": base["kind"], "sample": base["sample"]},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    from rocket_gb300 import synth
+    from rocket_gb300.engine import BatchBuilder, EngineConfig, PairEngine
+
+    wl = synth.workload(WORKLOAD)
+    N = len(wl)
+    n_pairs = N * (N - 1) // 2
+    stream = torch.cuda.current_stream(dev)
+    pinned = torch.from_numpy(wl.data).pin_memory()
+    seq = torch.empty(pinned.numel(), dtype=torch.uint8, device=dev)
+    seq.copy_(pinned)
+    builder = BatchBuilder("protein", 6, device=dev, max_batch=args.max_batch)
+    cfg = EngineConfig(wshift=args.wshift, fold=args.fold, items_per_cta=args.items_per_cta)
+    out = torch.zeros((N, N), dtype=torch.float64, device=dev)
+    out_host = torch.zeros((N, N), dtype=torch.float64).pin_memory()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    arena = None
+    engine = None
+    kernel_ms = []
+    state = {}
+
+    def step(record_kernel=False):
+        nonlocal arena, engine
+        arena = builder.build(seq, wl.offsets, arena=arena.reset() if arena is not None else None,
+                              stream=stream)
+        if engine is None:
+            engine = PairEngine(arena, cfg)
+        engine.arena = arena
+        engine.ensure_index(stream)
+        plan = engine.plan_triangle()
+        ev = None
+        if record_kernel:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        engine.run(plan, out, stream=stream, events=ev)
+        state["plan"] = plan
+        return ev
+
+    # warm-up
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    nnz = arena.nnz.copy()
+    plan = state["plan"]
+    alg_bytes = 0
+    rows = plan.rowids.cpu().numpy()
+    # algorithmic bytes of one pair launch: sum over pairs i<j of 8 (nnz_i + nnz_j)
+    alg_bytes = int(8 * (N - 1) * nnz.sum())
+
+    # timed device-resident steps
+    launches0 = builder.launches + engine.launches
+    step_ms = []
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index or 0) as clocks:
+        for s in range(args.steps):
+            flush.fill_(s & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ev = step(record_kernel=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            kernel_ms.append(ev[0].elapsed_time(ev[1]))
+    launches = (builder.launches + engine.launches - launches0) // args.steps
+    total_s = sum(step_ms) / 1000.0
+    total_s = _barrier_max(total_s, world)
+    value = world * args.steps * n_pairs / total_s
+
+    # end to end through the public API with host buffers
+    e2e_ms = []
+    h2d = int(wl.data.nbytes + wl.offsets.nbytes)
+    d2h = int(N * N * 8)
+    for s in range(max(1, args.steps)):
+        flush.fill_(s & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        seq.copy_(pinned, non_blocking=True)
+        step()
+        out_host.copy_(out, non_blocking=True)
+        stream.synchronize()
+        e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    e2e_s = _barrier_max(sum(e2e_ms) / 1000.0, world)
+    e2e_value = world * len(e2e_ms) * n_pairs / e2e_s
+
+    if rank != 0:
+        return 0
+    peak, peak_kind = _peaks()
+    k_ms = float(np.mean(kernel_ms))
+    achieved = alg_bytes / (k_ms / 1000.0) / 1e9
+    traffic = _traffic_per_launch()
+    line = {
+        "metric": "pairwise CV distances/s", "value": value, "unit": "pairs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD_TEXT,
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "flushed between steps (512 MB write, outside the timed events)",
+            "nnz_mean": float(nnz.mean()), "nnz_total": int(nnz.sum()),
+            "window_shift": args.wshift, "fold": args.fold, "items": plan.nitems,
+            "segments": plan.S,
+        },
+        "breakdown_ms": {"pair_kernel": k_ms, "step": float(np.mean(step_ms))},
+        "roofline": {
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "kernel": "k_allpairs",
+            "note": (f"{peak_kind} peak; algorithmic bytes 8*(nnz_i+nnz_j) per pair = "
+                     f"{alg_bytes / 1e9:.1f} GB per launch; frac > 1 = reuse of resident "
+                     "vectors in shared memory and L2, not DRAM bandwidth"),
+        },
+        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": float(np.mean(e2e_ms))},
+        "clocks": clocks.summary(),
+        "gpu_launches": int(launches),
+    }
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(wl, n_pairs, N, seconds=args.ref_seconds)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--wshift", type=int, default=10)
+    ap.add_argument("--fold", type=int, default=16)
+    ap.add_argument("--items-per-cta", type=int, default=4)
+    ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,162 @@
+/*
+ * phylogenetics.h -- C ABI of libphylogenetics.so (GB300 / sm_103a build).
+ *
+ * Drop-in for the library that Rocket's phylogenetics plug-in loads through
+ * JNA (Native.load("phylogenetics"),
+ * src/main/java/nl/esciencecenter/phylogenetics_analysis/Bindings.java:15).
+ *
+ * Conventions of every entry point (as the reference):
+ *   - device pointers and the stream are passed as uintptr_t;
+ *   - the caller owns every buffer, the stream and the current CUDA context;
+ *     the library never allocates, frees or selects a device;
+ *   - the return value is a cudaError_t code (0 = cudaSuccess); argument
+ *     errors print a message on stderr and return cudaErrorUnknown (999),
+ *     except where stated.
+ */
+#ifndef ROCKET_GB300_PHYLOGENETICS_H
+#define ROCKET_GB300_PHYLOGENETICS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------
+ * Drop-in boundary
+ * ------------------------------------------------------------------------- */
+
+/*
+ * Bytes of device scratch a CompositionVectorKernels instance allocates once
+ * and passes to every build and compare call.
+ * Replaces: native.cu:705-716 (estimateScratchMemory), bound at
+ * Bindings.java:17-20, called at CompositionVectorKernels.java:87.
+ * Any alphabet other than "DNA" is sized as "protein" (as the reference).
+ */
+long estimateScratchMemory(const char *alphabet, int k, int max_vector_size);
+
+/*
+ * Builds the composition vector of the residue string d_string[0, string_len):
+ * sorted keys (uint32, base-21 or base-4 K-mer codes) to d_keys, values
+ * (float, alpha / sqrt(sum alpha^2)) to d_values, the size to *set_size_ptr
+ * (host int), and pads [size, max_vector_size) with key 0xffffffff and value 0.
+ * Fails with cudaErrorUnknown if the size exceeds max_vector_size, if k is
+ * outside 3..10, if the keys would not fit 32 bits (protein k >= 8) or if the
+ * alphabet is neither "DNA" nor "protein".  Synchronous.
+ * Replaces: native.cu:718-752 (buildCompositionVector -> build_composition_vector
+ * native.cu:258-477), bound at Bindings.java:22-33, called at
+ * CompositionVectorKernels.java:91-112.
+ */
+int buildCompositionVector(uintptr_t stream, uintptr_t d_temp_storage_ptr, long temp_storage_size,
+                           const char *alphabet, int k, uintptr_t d_string_ptr, long string_len,
+                           uintptr_t d_set_keys_ptr, uintptr_t d_set_values_ptr,
+                           uintptr_t set_size_ptr, int max_vector_size);
+
+/*
+ * C = sum over keys present in both vectors of left_value * right_value,
+ * written as one double to d_output_ptr (device).  Synchronous.  Returns int:
+ * the Java binding's type (Bindings.java:35); the reference's C definition
+ * declares double (native.cu:755).
+ * Replaces: native.cu:755-780 (compareCompositionVectors ->
+ * calculate_cosine_similarity native.cu:645-703), bound at Bindings.java:35-45,
+ * called at CompositionVectorKernels.java:114-135.
+ */
+int compareCompositionVectors(uintptr_t stream, uintptr_t d_temp_storage_ptr, long temp_storage_size,
+                              uintptr_t d_left_keys_ptr, uintptr_t d_left_values_ptr, int left_size,
+                              uintptr_t d_right_keys_ptr, uintptr_t d_right_values_ptr,
+                              int right_size, uintptr_t d_output_ptr);
+
+/* ---------------------------------------------------------------------------
+ * Batched construction (new; the reference builds one proteome per call,
+ * driven per item by DeviceWorker.loadInput, DeviceWorker.java:118-157)
+ * ------------------------------------------------------------------------- */
+
+/* Scratch for building up to max_proteomes proteomes with at most
+ * max_candidates candidate slots in total; -1 on invalid arguments. */
+long phyloBuildBatchScratch(const char *alphabet, int k, int max_proteomes, long max_candidates);
+
+/* Phase 1: counting, candidate slots, Markov alpha, norms, per-proteome sizes.
+ * d_seq: concatenated residue bytes; d_seq_off: uint64[num_proteomes + 1].
+ * h_nnz (host int64[num_proteomes]) receives the vector sizes, h_candidates
+ * (host int64, may be 0) the total candidate slots.  Returns
+ * cudaErrorMemoryAllocation (2) when the slots exceed max_candidates (retry
+ * with *h_candidates).  Synchronous. */
+int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                        const char *alphabet, int k, int num_proteomes, uintptr_t d_seq,
+                        uintptr_t d_seq_off, long max_candidates, int64_t *h_nnz,
+                        int64_t *h_candidates);
+
+/* Phase 2 (same scratch and arguments as the Plan): vector p is written at
+ * d_keys/d_values[vec_off[p] ..] with vec_off[p] = arena_base + earlier sizes
+ * rounded up to 4 entries; d_vec_off (uint64[num_proteomes + 1]) receives the
+ * offsets; padding entries get key 0xffffffff, value 0.  Asynchronous. */
+int phyloBuildBatchEmit(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                        const char *alphabet, int k, int num_proteomes, long max_candidates,
+                        uintptr_t d_keys, uintptr_t d_values, uintptr_t d_vec_off,
+                        long arena_base);
+
+/* Norms (sum over entries of float(alpha)^2) of the last Plan, host double[]. */
+int phyloBuildBatchNorms(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                         const char *alphabet, int k, int num_proteomes, long max_candidates,
+                         double *h_norms);
+
+/* Dense (K-1)- and (K-2)-mer count tables and n0/n1/n2 of proteome p of the
+ * last Plan (host buffers of A^(K-1), A^(K-2) and 3 uint32). */
+int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                          const char *alphabet, int k, int num_proteomes, long max_candidates,
+                          int p, uint32_t *h_c1, uint32_t *h_c2, uint32_t *h_tot);
+
+/* Kernel launches (including memsets) one Plan + Emit issues. */
+int phyloBuildLaunchesPerBatch(void);
+
+/* ---------------------------------------------------------------------------
+ * Pair engine (new; the reference compares one pair per call,
+ * DeviceWorker.submitCorrelation, DeviceWorker.java:237-323)
+ * ------------------------------------------------------------------------- */
+
+/* Window index of an arena: d_roff uint32[num_vectors][num_windows + 1],
+ * entry [v][r] = number of entries of vector v with key < r << window_shift. */
+int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors,
+                     int window_shift, unsigned int num_windows, uintptr_t d_roff);
+
+/* Sets the pair kernel's shared-memory limit for this window width (4..11)
+ * and reports how many CTAs fit on one SM. */
+int phyloPairsPrepare(int window_shift, int *ctas_per_sm);
+
+/* Dynamic shared memory of the pair kernel for a window width. */
+int phyloPairsSmemBytes(int window_shift);
+
+/* Pair kernel over num_items work items (8 uint32 each: row0, nrow, col0,
+ * ncol, w0, w1, part, tile); d_counter (uint32) must be 0; partial blocks of
+ * 16 x 256 float pairs go to d_part; d_item_cycles (int64[num_items]) may be 0.
+ * Asynchronous. */
+int phyloPairsLaunch(uintptr_t stream, uintptr_t d_keys, uintptr_t d_values, uintptr_t d_vec_off,
+                     uintptr_t d_roff, unsigned int num_windows, int window_shift,
+                     uintptr_t d_rowids, uintptr_t d_colids, uintptr_t d_items, int num_items,
+                     uintptr_t d_counter, uintptr_t d_part, int fold, uintptr_t d_item_cycles,
+                     int grid);
+
+/* Sums the partial blocks of each tile (4 uint32: row0, nrow, col0, ncol) into
+ * d_out[rowid * ldc + colid] (double); `upper` keeps pairs whose row position
+ * is below the column position, `mirror` also writes the transposed entry. */
+int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
+                     int segments, uintptr_t d_rowids, uintptr_t d_colids, uintptr_t d_out,
+                     long ldc, int upper, int mirror);
+
+/* d_out[v * ldc + v] = sum of squares of vector v (the diagonal the
+ * reference's run includes, phylogenetics_analysis/Main.java:196). */
+int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int num_vectors,
+                 uintptr_t d_out, long ldc);
+
+/* compareCompositionVectors without the synchronisation (result left on the
+ * device); scratch from estimateScratchMemory. */
+int phyloComparePairAsync(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                          uintptr_t d_left_keys, uintptr_t d_left_values, int left_size,
+                          uintptr_t d_right_keys, uintptr_t d_right_values, int right_size,
+                          uintptr_t d_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ROCKET_GB300_PHYLOGENETICS_H */

@@ -1,0 +1,67 @@
+// allpairs.cuh -- batched pair engine (declarations).
+#pragma once
+#include "common.cuh"
+
+namespace phylo {
+
+constexpr int AP_TI = 16;             // row vectors per item (densified in shared memory)
+constexpr int AP_THREADS = 256;       // one column vector per thread
+constexpr int AP_TJ = AP_THREADS;     // column vectors per item
+
+// One unit of work: up to 16 row vectors x 256 column vectors over the key
+// windows [w0, w1).  Vectors are named by positions in rowids / colids.
+struct ApItem {
+    uint32_t row0, nrow;  // rows: rowids[row0 .. row0 + nrow)
+    uint32_t col0, ncol;  // columns: colids[col0 .. col0 + ncol)
+    uint32_t w0, w1;      // key windows
+    uint32_t part;        // index of this item's 16 x 256 partial block
+    uint32_t tile;        // tile this item contributes to
+};
+
+struct ApArgs {
+    const uint32_t *keys;
+    const float *vals;
+    const uint64_t *vec_off;   // [N+1] arena offsets, each a multiple of 4 entries
+    const uint32_t *roff;      // [N][R+1] window index
+    uint32_t R;                // windows per vector
+    uint32_t wshift;           // window width = 1 << wshift keys
+    const uint32_t *rowids, *colids;
+    const ApItem *items;
+    uint32_t nitems;
+    uint32_t *counter;         // work counter (zeroed before launch)
+    FF *part;                  // [parts][AP_TI][AP_TJ]
+    uint32_t fold;             // products per accumulator between compensated folds
+    int64_t *item_cycles;      // optional per-item clock64 durations (may be null)
+};
+
+size_t ap_smem_bytes(uint32_t wshift);
+int ap_max_wshift();
+cudaError_t ap_prepare(uint32_t wshift, int *ctas_per_sm);
+cudaError_t ap_launch(const ApArgs &a, int grid, cudaStream_t st);
+
+// window index: roff[v][r] = number of entries of vector v with key < r << wshift
+cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
+                               uint32_t R, uint32_t wshift, uint32_t *roff, cudaStream_t st);
+
+// Tile t (rows rowids[row0..], columns colids[col0..]) has S partial blocks
+// part[t * S + s].  Writes out[rowid * ldc + colid] (and the mirrored entry
+// when `mirror`), for pairs with row position < column position when `upper`.
+struct ApTile {
+    uint32_t row0, nrow, col0, ncol;
+};
+struct ApReduceArgs {
+    const FF *part;
+    const ApTile *tiles;
+    uint32_t ntiles, S;
+    const uint32_t *rowids, *colids;
+    double *out;
+    uint64_t ldc;
+    int upper, mirror;
+};
+cudaError_t ap_reduce_launch(const ApReduceArgs &r, cudaStream_t st);
+
+// C of each vector with itself (sum of squares, float-float): out[v*ldc+v].
+cudaError_t self_dot_launch(const float *vals, const uint64_t *vec_off, uint32_t N, double *out,
+                            uint64_t ldc, cudaStream_t st);
+
+}  // namespace phylo

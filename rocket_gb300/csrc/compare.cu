@@ -1,0 +1,313 @@
+// compare.cu -- sparse cosine of one pair of composition vectors.
+//
+// C = sum over keys present in both lists of a * b, the quantity the reference
+// computes with a merge-path partition and one merge step per thread
+// (phylogenetics/src/main/cpp/native.cu:513-703).  This version:
+//
+//   * k_partition: one warp per tile boundary finds the merge-path split of
+//     diagonal t*TILE by a 32-ary search (about five dependent global loads
+//     instead of twenty), ties going to the left list as in native.cu:529.
+//     It also resets the completion ticket and the status word.
+//   * k_intersect: persistent CTAs walk contiguous runs of tiles.  For each
+//     tile a single thread issues 1-D bulk copies (TMA) of the left and right
+//     key/value ranges into shared memory, double-buffered on mbarriers; all
+//     threads then run a per-thread merge-path over 16 diagonals in shared
+//     memory.  Products are split exactly (TwoProduct) and summed as
+//     float-float (TwoSum); warp shuffles and one shared-memory step reduce
+//     the CTA, and the last CTA combines the per-CTA partials in a fixed
+//     order into the double result.
+//
+// Ranges need not be 16-byte aligned: each copy is widened to 16-byte
+// boundaries (never leaving the 16-byte block of a valid element) and the
+// consumer indexes from the offset.
+#include "compare.cuh"
+
+namespace phylo {
+
+constexpr int CMP_THREADS = 256;
+constexpr int CMP_IPT = 16;
+constexpr int CMP_TILE = CMP_THREADS * CMP_IPT;  // merged elements per tile
+constexpr int CMP_BUF = CMP_TILE + 16;           // entries per stage per type (A part + B part)
+constexpr int CMP_MAX_CTAS = 1024;
+
+struct CmpState {
+    FF partial[CMP_MAX_CTAS];
+    uint32_t ticket;
+    uint32_t status;
+};
+
+size_t compare_scratch_bytes(uint64_t max_total) {
+    uint64_t ntiles = div_up(max_total, CMP_TILE) + 1;
+    return scratch_bytes<uint32_t>(ntiles + 1) + scratch_bytes<CmpState>(1);
+}
+
+// i = number of left elements before merged position d (ties to the left list).
+__device__ __forceinline__ uint32_t warp_merge_path(uint64_t d, const uint32_t *__restrict__ A,
+                                                    uint32_t na, const uint32_t *__restrict__ B,
+                                                    uint32_t nb) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t lo = d > nb ? (uint32_t)(d - nb) : 0u;
+    uint32_t hi = d < na ? (uint32_t)d : na;
+    while (hi > lo) {
+        const uint32_t span = hi - lo;
+        const uint32_t step = (span + 31) / 32;
+        const uint64_t i = (uint64_t)lo + (uint64_t)(lane + 1) * step;
+        bool p = false;
+        if (i <= hi) p = __ldg(&A[i - 1]) <= __ldg(&B[d - i]);
+        const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, p));
+        const uint64_t nlo = (uint64_t)lo + (uint64_t)cnt * step;
+        const uint64_t nhi = (uint64_t)lo + (uint64_t)(cnt + 1) * step - 1;
+        lo = (uint32_t)nlo;
+        hi = nhi < hi ? (uint32_t)nhi : hi;
+    }
+    return lo;
+}
+
+__global__ void k_partition(const uint32_t *__restrict__ A, uint32_t na,
+                            const uint32_t *__restrict__ B, uint32_t nb, uint32_t ntiles,
+                            uint32_t *splits, CmpState *st) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->ticket = 0;
+        st->status = 0;
+    }
+    const uint32_t t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (t > ntiles) return;
+    uint64_t d = (uint64_t)t * CMP_TILE;
+    const uint64_t total = (uint64_t)na + nb;
+    if (d > total) d = total;
+    const uint32_t i = warp_merge_path(d, A, na, B, nb);
+    if ((threadIdx.x & 31) == 0) splits[t] = i;
+}
+
+struct Stage {
+    uint32_t ka_off, va_off, kb_off, vb_off;  // element offsets of the first wanted entry
+    uint32_t na, nb;
+};
+
+// Issues the bulk copies of tile `t` into buffer `buf`; returns the stage layout.
+__device__ __forceinline__ Stage issue_tile(uint32_t t, const uint32_t *splits, uint64_t total,
+                                            const uint32_t *Ak, const float *Av,
+                                            const uint32_t *Bk, const float *Bv, uint32_t *sk,
+                                            float *sv, uint64_t *bar, bool issue) {
+    Stage s;
+    const uint64_t d0 = (uint64_t)t * CMP_TILE;
+    const uint64_t d1 = min(d0 + CMP_TILE, total);
+    const uint32_t i0 = splits[t], i1 = splits[t + 1];
+    const uint32_t j0 = (uint32_t)(d0 - i0), j1 = (uint32_t)(d1 - i1);
+    s.na = i1 - i0;
+    s.nb = j1 - j0;
+    // widened byte ranges
+    const uintptr_t ka0 = (uintptr_t)(Ak + i0), ka1 = (uintptr_t)(Ak + i1);
+    const uintptr_t va0 = (uintptr_t)(Av + i0), va1 = (uintptr_t)(Av + i1);
+    const uintptr_t kb0 = (uintptr_t)(Bk + j0), kb1 = (uintptr_t)(Bk + j1);
+    const uintptr_t vb0 = (uintptr_t)(Bv + j0), vb1 = (uintptr_t)(Bv + j1);
+    auto lo16 = [](uintptr_t x) { return x & ~(uintptr_t)15; };
+    auto hi16 = [](uintptr_t x) { return (x + 15) & ~(uintptr_t)15; };
+    const uint32_t bka = s.na ? (uint32_t)(hi16(ka1) - lo16(ka0)) : 0u;
+    const uint32_t bva = s.na ? (uint32_t)(hi16(va1) - lo16(va0)) : 0u;
+    const uint32_t bkb = s.nb ? (uint32_t)(hi16(kb1) - lo16(kb0)) : 0u;
+    const uint32_t bvb = s.nb ? (uint32_t)(hi16(vb1) - lo16(vb0)) : 0u;
+    // B part starts after the A part (both multiples of 16 bytes)
+    s.ka_off = (uint32_t)((ka0 & 15) >> 2);
+    s.va_off = (uint32_t)((va0 & 15) >> 2);
+    s.kb_off = bka / 4 + (uint32_t)((kb0 & 15) >> 2);
+    s.vb_off = bva / 4 + (uint32_t)((vb0 & 15) >> 2);
+    if (issue) {
+        mbar_arrive_expect_tx(bar, bka + bva + bkb + bvb);
+        if (bka) bulk_g2s(sk, (const void *)lo16(ka0), bka, bar);
+        if (bva) bulk_g2s(sv, (const void *)lo16(va0), bva, bar);
+        if (bkb) bulk_g2s(sk + bka / 4, (const void *)lo16(kb0), bkb, bar);
+        if (bvb) bulk_g2s(sv + bva / 4, (const void *)lo16(vb0), bvb, bar);
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(CMP_THREADS) k_intersect(
+    const uint32_t *__restrict__ Ak, const float *__restrict__ Av, uint32_t na,
+    const uint32_t *__restrict__ Bk, const float *__restrict__ Bv, uint32_t nb,
+    const uint32_t *__restrict__ splits, uint32_t ntiles, CmpState *st, double *out) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    uint32_t *sk[2];
+    float *sv[2];
+    sk[0] = (uint32_t *)smem_raw;
+    sv[0] = (float *)(sk[0] + CMP_BUF);
+    sk[1] = (uint32_t *)(sv[0] + CMP_BUF);
+    sv[1] = (float *)(sk[1] + CMP_BUF);
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ FF warp_part[CMP_THREADS / 32];
+    __shared__ bool s_last;
+    __shared__ bool s_fail;
+
+    const uint64_t total = (uint64_t)na + nb;
+    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t_begin = blockIdx.x * per;
+    const uint32_t t_end = min(ntiles, t_begin + per);
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        s_fail = false;
+    }
+    __syncthreads();
+
+    FF acc = {0.0f, 0.0f};
+    Stage stg0 = {0, 0, 0, 0, 0, 0}, stg1 = {0, 0, 0, 0, 0, 0};
+    // prologue: tiles t_begin, t_begin+1
+    if (t_begin < t_end)
+        stg0 = issue_tile(t_begin, splits, total, Ak, Av, Bk, Bv, sk[0], sv[0], &bar[0],
+                          threadIdx.x == 0);
+    if (t_begin + 1 < t_end)
+        stg1 = issue_tile(t_begin + 1, splits, total, Ak, Av, Bk, Bv, sk[1], sv[1], &bar[1],
+                          threadIdx.x == 0);
+    uint32_t fail_at = 0xffffffffu;
+    for (uint32_t t = t_begin; t < t_end; t++) {
+        const int b = (t - t_begin) & 1;
+        const uint32_t phase = ((t - t_begin) >> 1) & 1;
+        if (!mbar_wait_bounded(&bar[b], phase)) s_fail = true;
+        __syncthreads();
+        if (s_fail) {
+            fail_at = t;
+            break;
+        }
+        const Stage s = b ? stg1 : stg0;
+        uint32_t *skb = b ? sk[1] : sk[0];
+        float *svb = b ? sv[1] : sv[0];
+        const uint32_t *ka = skb + s.ka_off;
+        const float *va = svb + s.va_off;
+        const uint32_t *kb = skb + s.kb_off;
+        const float *vb = svb + s.vb_off;
+        // per-thread merge path inside the tile
+        const uint32_t d = threadIdx.x * CMP_IPT;
+        const uint32_t n = s.na + s.nb;
+        if (d < n) {
+            uint32_t lo = d > s.nb ? d - s.nb : 0u;
+            uint32_t hi = d < s.na ? d : s.na;
+            while (lo < hi) {
+                uint32_t mid = (lo + hi) / 2 + 1;
+                if (ka[mid - 1] <= kb[d - mid]) lo = mid; else hi = mid - 1;
+            }
+            uint32_t i = lo, j = d - lo;
+            const uint32_t steps = min((uint32_t)CMP_IPT, n - d);
+            for (uint32_t it = 0; it < steps; it++) {
+                const bool has_a = i < s.na, has_b = j < s.nb;
+                const uint32_t x = has_a ? ka[i] : 0u, y = has_b ? kb[j] : 0u;
+                const bool take_a = has_a && (!has_b || x <= y);
+                if (take_a && has_b && x == y) {
+                    float p, e;
+                    two_prod(va[i], vb[j], p, e);
+                    ff_add(acc, p);
+                    acc.lo = __fadd_rn(acc.lo, e);
+                }
+                i += take_a;
+                j += !take_a;
+            }
+        }
+        __syncthreads();  // everyone done with buffer b
+        const uint32_t tn = t + 2;
+        if (tn < t_end) {
+            if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const Stage ns = issue_tile(tn, splits, total, Ak, Av, Bk, Bv, skb, svb, &bar[b],
+                                        threadIdx.x == 0);
+            if (b) stg1 = ns; else stg0 = ns;
+        }
+    }
+    if (fail_at != 0xffffffffu) {
+        // record the failure, then wait (bounded) for the copies that may still
+        // be in flight: the failed tile and the one issued after it
+        if (threadIdx.x == 0) atomicOr(&st->status, (uint32_t)DEV_WAIT_TIMEOUT);
+        for (uint32_t t = fail_at; t < t_end && t < fail_at + 2; t++) {
+            const uint32_t rel = t - t_begin;
+            (void)mbar_wait_bounded(&bar[rel & 1], (rel >> 1) & 1, 1u << 16);
+        }
+        __syncthreads();
+    }
+    // CTA reduction
+    acc = ff_warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) warp_part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        FF r = {0.0f, 0.0f};
+        for (int w = 0; w < CMP_THREADS / 32; w++) r = ff_merge(r, warp_part[w]);
+        st->partial[blockIdx.x] = r;
+        __threadfence();
+        const uint32_t done = atomicAdd(&st->ticket, 1u);
+        s_last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x < 32) {
+        __threadfence();
+        // fixed order: lane l sums partials l, l+32, ... in double-double
+        DD dacc = {0.0, 0.0};
+        for (uint32_t c = threadIdx.x; c < gridDim.x; c += 32) {
+            const volatile float *pp = reinterpret_cast<volatile float *>(&st->partial[c]);
+            dd_add(dacc, (double)pp[0]);
+            dd_add(dacc, (double)pp[1]);
+        }
+#pragma unroll
+        for (int dd = 16; dd > 0; dd >>= 1) {
+            DD o;
+            o.hi = __shfl_down_sync(0xffffffffu, dacc.hi, dd);
+            o.lo = __shfl_down_sync(0xffffffffu, dacc.lo, dd);
+            dacc = dd_merge(dacc, o);
+        }
+        if (threadIdx.x == 0) *out = __dadd_rn(dacc.hi, dacc.lo);
+    }
+}
+
+static int compare_grid(uint32_t ntiles) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    uint32_t g = ntiles < (uint32_t)sms * 3 ? ntiles : (uint32_t)sms * 3;
+    if (g > CMP_MAX_CTAS) g = CMP_MAX_CTAS;
+    return g ? (int)g : 1;
+}
+
+static const size_t kCmpSmem = sizeof(uint32_t) * CMP_BUF * 4;
+
+cudaError_t compare_launch(cudaStream_t stream, void *scratch, size_t scratch_size,
+                           const uint32_t *lk, const float *lv, uint32_t nl, const uint32_t *rk,
+                           const float *rv, uint32_t nr, double *d_out, uint32_t **status_out) {
+    const uint64_t total = (uint64_t)nl + nr;
+    const uint32_t ntiles = (uint32_t)div_up(total, CMP_TILE);
+    Scratch sc(scratch, scratch_size);
+    uint32_t *splits = sc.take<uint32_t>((uint64_t)ntiles + 1 + 1);
+    CmpState *st = sc.take<CmpState>(1);
+    if (!splits || !st) {
+        fprintf(stderr,
+                "phylogenetics: scratch of %zu bytes too small to compare vectors of sizes %u and "
+                "%u\n",
+                scratch_size, nl, nr);
+        return cudaErrorInvalidValue;
+    }
+    if (status_out) *status_out = &st->status;
+    {
+        static uint64_t attr_done = 0;  // one bit per device
+        int dev = 0;
+        PHYLO_CHECK(cudaGetDevice(&dev));
+        if (dev < 64 && !(attr_done >> dev & 1)) {
+            PHYLO_CHECK(cudaFuncSetAttribute(
+                k_intersect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCmpSmem));
+            attr_done |= 1ull << dev;
+        }
+    }
+    const int warps_per_cta = 8;
+    const uint32_t pgrid = (ntiles + 1 + warps_per_cta - 1) / warps_per_cta;
+    k_partition<<<pgrid, warps_per_cta * 32, 0, stream>>>(lk, nl, rk, nr, ntiles, splits, st);
+    if (ntiles == 0) {
+        // empty: C = 0
+        PHYLO_CHECK(cudaMemsetAsync(d_out, 0, sizeof(double), stream));
+        return cudaGetLastError();
+    }
+    const int grid = compare_grid(ntiles);
+    k_intersect<<<grid, CMP_THREADS, kCmpSmem, stream>>>(lk, lv, nl, rk, rv, nr, splits, ntiles,
+                                                        st, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace phylo

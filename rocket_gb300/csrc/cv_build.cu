@@ -1,0 +1,578 @@
+// cv_build.cu -- composition-vector construction on the device.
+//
+// Same result as the reference pipeline of phylogenetics/src/main/cpp/native.cu
+// (count_kmers :220-256, totals :317-345, Markov alpha :350-400, nnz/norm
+// :402-428, sorted selection :449-458, normalisation :460-468, padding
+// :470-474), computed without the dense A^K table:
+//
+//   A slot a.m.b (a, b single symbols, m the (K-2)-mer in between) can only be
+//   nonzero when its prefix a.m and its suffix m.b were both seen as
+//   (K-1)-mers (then the middle m was seen too).  So the candidates are, for
+//   every seen (K-1)-mer q = a.m in ascending order, the symbols b of the
+//   right-extension set R(m) = { b : m.b seen }, kept as a 21-bit mask per
+//   (K-2)-mer.  Enumerated in that order the candidate keys q*A + b are
+//   already sorted, and the count of every seen K-mer is scattered straight
+//   into its candidate slot (rank of b in R(m)) -- no sort and no A^K table.
+//
+// Pipeline per batch of proteomes (all kernels take the whole batch):
+//   k_prep          tile bases per proteome
+//   k_count         (K-2)/(K-1) counts, right-extension masks, window totals
+//   k_cand_count    candidates per chunk of 2048 (K-1)-mers
+//   scan            -> global candidate offsets
+//   k_cand_offsets  per-(K-1)-mer candidate offsets
+//   k_c0_zero/k_c0_scatter   K-mer counts into candidate slots
+//   k_alpha         Markov alpha (reference double order), survivor counts,
+//                   exact-ish norm partials (double-double)
+//   scan            -> output offsets
+//   k_norm          per-proteome norm, scale, nnz
+//   (host reads nnz, checks capacity)
+//   k_compact       survivors' keys and normalised values, sorted
+#include "cv_build.cuh"
+#include "scan.cuh"
+
+namespace phylo {
+
+constexpr int TILE = 2048;           // sequence positions per counting tile
+constexpr int COUNT_THREADS = 256;
+constexpr int CH = 2048;             // (K-1)-mers per chunk
+constexpr int CHUNK_THREADS = 256;
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int find_owner(const uint64_t *__restrict__ base, int n, uint64_t t) {
+    // largest p with base[p] <= t, base has n+1 entries, base[0] = 0
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (base[mid] <= t) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Markov alpha with the reference's operation order (native.cu:387-394):
+//   p  = full / n0
+//   p0 = ((prefix / n1) * (suffix / n1)) / (middle / n2)
+//   alpha = float((p - p0) / p0)
+// Every operation is an explicitly rounded IEEE double op, so no FMA
+// contraction can change the result.
+__device__ __forceinline__ float markov_alpha(uint32_t full, uint32_t prefix, uint32_t suffix,
+                                              uint32_t middle, uint32_t n0, uint32_t n1,
+                                              uint32_t n2) {
+    if (full == 0u && n0 != 0u) return -1.0f;  // (0 - p0) / p0 == -1 exactly (p0 > 0 finite)
+    double p = __ddiv_rn((double)full, (double)n0);
+    double pp = __ddiv_rn((double)prefix, (double)n1);
+    double ps = __ddiv_rn((double)suffix, (double)n1);
+    double pm = __ddiv_rn((double)middle, (double)n2);
+    double p0 = __ddiv_rn(__dmul_rn(pp, ps), pm);
+    return __double2float_rn(__ddiv_rn(__dsub_rn(p, p0), p0));
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// tile_base[p] = number of TILE-sized tiles of proteomes < p; tile_base[B] = total.
+__global__ void k_prep(int B, const uint64_t *__restrict__ seq_off, uint64_t *tile_base) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        uint64_t acc = 0;
+        for (int p = 0; p < B; p++) {
+            tile_base[p] = acc;
+            acc += div_up(seq_off[p + 1] - seq_off[p], TILE);
+        }
+        tile_base[B] = acc;
+    }
+}
+
+// Counts (K-2)- and (K-1)-windows, marks right extensions, totals n0/n1/n2.
+// A window starting at i counts for length L when its L symbols are all in the
+// alphabet and inside the proteome (native.cu:236-252).
+__global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
+    __shared__ uint8_t dig[TILE + 16];
+    __shared__ uint32_t ntot[3];
+    const int K = a.k;
+    const uint32_t A = a.A;
+    const uint64_t total_tiles = a.tile_base[a.B];
+    for (uint64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+        const int p = find_owner(a.tile_base, a.B, t);
+        const uint64_t s0 = a.seq_off[p], len = a.seq_off[p + 1] - s0;
+        const uint64_t start = (t - a.tile_base[p]) * TILE;
+        if (threadIdx.x < 3) ntot[threadIdx.x] = 0;
+        for (int j = threadIdx.x; j < TILE + K; j += COUNT_THREADS) {
+            uint64_t pos = start + j;
+            dig[j] = pos < len ? (uint8_t)char_to_digit(a.alpha, a.seq[s0 + pos]) : (uint8_t)0xff;
+        }
+        __syncthreads();
+        uint32_t *c1 = a.c1 + (uint64_t)p * a.T1;
+        uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
+        uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+        uint32_t cnt0 = 0, cnt1 = 0, cnt2 = 0;
+        for (int u = 0; u < TILE / COUNT_THREADS; u++) {
+            const int li = u * COUNT_THREADS + threadIdx.x;
+            const bool inb = start + li < len;
+            uint32_t w = 0, w2 = 0, w1 = 0, last = 0;
+            int run = 0;
+            if (inb) {
+                for (int j = 0; j < K; j++) {
+                    uint32_t d = dig[li + j];
+                    if (d == 0xffu) break;
+                    w = w * A + d;
+                    run = j + 1;
+                    if (j == K - 3) w2 = w;
+                    if (j == K - 2) { w1 = w; last = d; }
+                }
+            }
+            const bool v2 = run >= K - 2, v1 = run >= K - 1, v0 = run >= K;
+            cnt2 += v2; cnt1 += v1; cnt0 += v0;
+            // (K-2)-mer counts, aggregated over equal keys within the warp
+            unsigned act = __ballot_sync(0xffffffffu, v2);
+            if (v2) {
+                unsigned peers = __match_any_sync(act, w2);
+                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&c2[w2], __popc(peers));
+            }
+            act = __ballot_sync(0xffffffffu, v1);
+            if (v1) {
+                unsigned peers = __match_any_sync(act, w1);
+                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&c1[w1], __popc(peers));
+                const uint32_t bit = 1u << last;
+                if (!(__ldcg(&mk[w2]) & bit)) atomicOr(&mk[w2], bit);
+            }
+        }
+        // totals
+        cnt0 = __reduce_add_sync(0xffffffffu, cnt0);
+        cnt1 = __reduce_add_sync(0xffffffffu, cnt1);
+        cnt2 = __reduce_add_sync(0xffffffffu, cnt2);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&ntot[0], cnt0);
+            atomicAdd(&ntot[1], cnt1);
+            atomicAdd(&ntot[2], cnt2);
+        }
+        __syncthreads();
+        if (threadIdx.x < 3 && ntot[threadIdx.x]) atomicAdd(&a.tot[p * 4 + threadIdx.x], ntot[threadIdx.x]);
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ uint32_t cand_count_of(const BuildArgs &a, int p, uint64_t q) {
+    if (q >= a.T1) return 0;
+    uint32_t c = a.c1[(uint64_t)p * a.T1 + q];
+    if (!c) return 0;
+    return __popc(a.mask[(uint64_t)p * a.T2 + (q % a.T2)]);
+}
+
+// Candidates per chunk of CH (K-1)-mers.  grid = (NCH, B)
+__global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
+    const int p = blockIdx.y, c = blockIdx.x;
+    const uint64_t q0 = (uint64_t)c * CH;
+    uint32_t s = 0;
+    for (int i = threadIdx.x; i < CH; i += CHUNK_THREADS) s += cand_count_of(a, p, q0 + i);
+    s = __reduce_add_sync(0xffffffffu, s);
+    __shared__ uint32_t ws[CHUNK_THREADS / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < CHUNK_THREADS / 32; w++) t += ws[w];
+        a.chunk_cand[(uint64_t)p * a.NCH + c] = t;
+    }
+}
+
+// coff[p][q] = candidate offset of (K-1)-mer q within proteome p.  grid = (NCH, B)
+__global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
+    __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
+    const int p = blockIdx.y, c = blockIdx.x;
+    const uint64_t pc = (uint64_t)p * a.NCH + c;
+    const uint64_t q0 = (uint64_t)c * CH;
+    constexpr int PER = CH / CHUNK_THREADS;
+    uint32_t v[PER];
+    uint64_t s = 0;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        v[i] = cand_count_of(a, p, q0 + threadIdx.x * PER + i);
+        s += v[i];
+    }
+    uint64_t tot;
+    uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
+    uint64_t base = a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH];
+    uint32_t *coff = a.coff + (uint64_t)p * a.T1;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        uint64_t q = q0 + threadIdx.x * PER + i;
+        if (q < a.T1) coff[q] = (uint32_t)(base + ex);
+        ex += v[i];
+    }
+}
+
+// zero the K-mer count slots of all candidates (bounded by capacity)
+__global__ void k_c0_zero(BuildArgs a) {
+    uint64_t total = a.chunk_cand_off[(uint64_t)a.B * a.NCH];
+    if (total > a.cand_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
+        total = a.cand_cap;
+    }
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        a.c0a[i] = 0;
+}
+
+// Every K-window adds one to the slot of its candidate (native.cu:244).
+__global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
+    __shared__ uint8_t dig[TILE + 16];
+    const int K = a.k;
+    const uint32_t A = a.A;
+    const uint64_t total_tiles = a.tile_base[a.B];
+    for (uint64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+        const int p = find_owner(a.tile_base, a.B, t);
+        const uint64_t s0 = a.seq_off[p], len = a.seq_off[p + 1] - s0;
+        const uint64_t start = (t - a.tile_base[p]) * TILE;
+        for (int j = threadIdx.x; j < TILE + K; j += COUNT_THREADS) {
+            uint64_t pos = start + j;
+            dig[j] = pos < len ? (uint8_t)char_to_digit(a.alpha, a.seq[s0 + pos]) : (uint8_t)0xff;
+        }
+        __syncthreads();
+        const uint32_t *coff = a.coff + (uint64_t)p * a.T1;
+        const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+        const uint64_t cbase = a.chunk_cand_off[(uint64_t)p * a.NCH];
+        for (int u = 0; u < TILE / COUNT_THREADS; u++) {
+            const int li = u * COUNT_THREADS + threadIdx.x;
+            bool v0 = false;
+            uint64_t slot = 0;
+            if (start + li < len) {
+                uint32_t w = 0;
+                int j;
+                for (j = 0; j < K - 1; j++) {
+                    uint32_t d = dig[li + j];
+                    if (d == 0xffu) break;
+                    w = w * A + d;
+                }
+                if (j == K - 1) {
+                    uint32_t b = dig[li + K - 1];
+                    if (b != 0xffu) {
+                        v0 = true;
+                        uint32_t m = w % (uint32_t)a.T2;
+                        slot = cbase + coff[w] + __popc(mk[m] & ((1u << b) - 1u));
+                    }
+                }
+            }
+            unsigned act = __ballot_sync(0xffffffffu, v0);
+            if (v0) {
+                unsigned peers = __match_any_sync(act, slot);
+                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && slot < a.cand_cap)
+                    atomicAdd(&a.c0a[slot], __popc(peers));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Locate candidate u (chunk-local) -> (K-1)-mer q, symbol b.
+struct ChunkCtx {
+    uint64_t q0;
+    uint32_t nq;
+};
+
+__device__ __forceinline__ void locate(const uint32_t *sm_off, uint32_t nq, uint32_t u,
+                                       uint32_t &ql, uint32_t &r) {
+    // largest ql with sm_off[ql] <= u
+    uint32_t lo = 0, hi = nq;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (sm_off[mid] <= u) lo = mid; else hi = mid;
+    }
+    ql = lo;
+    r = u - sm_off[lo];
+}
+
+// Markov alpha for every candidate; alpha bits replace the count in place
+// (as native.cu:399 does); per-chunk survivor counts and norm partials.
+// grid = (NCH, B)
+__global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
+    __shared__ uint32_t sm_off[CH];
+    __shared__ double s_hi[CHUNK_THREADS / 32], s_lo[CHUNK_THREADS / 32];
+    __shared__ uint32_t s_surv[CHUNK_THREADS / 32], s_m1[CHUNK_THREADS / 32];
+    const int p = blockIdx.y, c = blockIdx.x;
+    const uint64_t pc = (uint64_t)p * a.NCH + c;
+    const uint64_t cb = a.chunk_cand_off[pc];
+    const uint32_t ncand = (uint32_t)(a.chunk_cand_off[pc + 1] - cb);
+    const uint64_t q0 = (uint64_t)c * CH;
+    const uint32_t nq = (uint32_t)min((uint64_t)CH, a.T1 - q0);
+    const uint32_t *coff = a.coff + (uint64_t)p * a.T1;
+    const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1;
+    const uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
+    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+    const uint32_t n0 = a.tot[p * 4 + 0], n1 = a.tot[p * 4 + 1], n2 = a.tot[p * 4 + 2];
+    uint32_t local0 = ncand ? coff[q0] : 0;
+    for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
+    __syncthreads();
+    DD acc = {0.0, 0.0};
+    uint32_t surv = 0, m1 = 0;
+    const uint32_t A = a.A;
+    for (uint32_t u = threadIdx.x; u < ncand; u += CHUNK_THREADS) {
+        if (cb + u >= a.cand_cap) break;
+        uint32_t ql, r;
+        locate(sm_off, nq, u, ql, r);
+        const uint64_t q = q0 + ql;
+        const uint32_t m = (uint32_t)(q % a.T2);
+        const uint32_t b = nth_set_bit(mk[m], r);
+        const uint32_t full = a.c0a[cb + u];
+        const uint32_t pre = c1[q];
+        const uint32_t suf = c1[(uint64_t)m * A + b];
+        const uint32_t mid = c2[m];
+        const float f = markov_alpha(full, pre, suf, mid, n0, n1, n2);
+        const uint32_t bits = __float_as_uint(f);
+        a.c0a[cb + u] = bits;
+        if (bits != 0u) {
+            surv++;
+            const float sq = __fmul_rn(f, f);
+            if (sq == 1.0f) m1++;
+            else dd_add(acc, (double)sq);
+        }
+    }
+    // reduce
+    surv = __reduce_add_sync(0xffffffffu, surv);
+    m1 = __reduce_add_sync(0xffffffffu, m1);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        DD o;
+        o.hi = __shfl_down_sync(0xffffffffu, acc.hi, d);
+        o.lo = __shfl_down_sync(0xffffffffu, acc.lo, d);
+        acc = dd_merge(acc, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_hi[w] = acc.hi; s_lo[w] = acc.lo; s_surv[w] = surv; s_m1[w] = m1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        DD t = {0.0, 0.0};
+        uint32_t ts = 0, tm = 0;
+        for (int i = 0; i < CHUNK_THREADS / 32; i++) {
+            t = dd_merge(t, DD{s_hi[i], s_lo[i]});
+            ts += s_surv[i];
+            tm += s_m1[i];
+        }
+        a.chunk_surv[pc] = ts;
+        a.chunk_m1[pc] = tm;
+        a.chunk_nhi[pc] = t.hi;
+        a.chunk_nlo[pc] = t.lo;
+    }
+}
+
+// Per proteome: norm (fixed chunk order), scale = sqrt(norm), nnz.  grid = B, 32 threads.
+__global__ void k_norm(BuildArgs a) {
+    const int p = blockIdx.x;
+    const int lane = threadIdx.x;
+    DD acc = {0.0, 0.0};
+    uint64_t m1 = 0;
+    for (uint64_t c = lane; c < a.NCH; c += 32) {
+        const uint64_t pc = (uint64_t)p * a.NCH + c;
+        acc = dd_merge(acc, DD{a.chunk_nhi[pc], a.chunk_nlo[pc]});
+        m1 += a.chunk_m1[pc];
+    }
+    // fixed-order tree over lanes
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        DD o;
+        o.hi = __shfl_down_sync(0xffffffffu, acc.hi, d);
+        o.lo = __shfl_down_sync(0xffffffffu, acc.lo, d);
+        acc = dd_merge(acc, o);
+        m1 += __shfl_down_sync(0xffffffffu, m1, d);
+    }
+    if (lane == 0) {
+        // exact integer count of unit squares, then the rest
+        DD n = {(double)m1, 0.0};
+        n = dd_merge(n, acc);
+        const double norm = __dadd_rn(n.hi, n.lo);
+        const double scale = __dsqrt_rn(norm);
+        a.norm[p] = norm;
+        a.scale[p] = scale;
+        const uint64_t o0 = a.chunk_out_off[(uint64_t)p * a.NCH];
+        const uint64_t o1 = a.chunk_out_off[(uint64_t)(p + 1) * a.NCH];
+        a.nnz[p] = o1 - o0;
+        a.out_base[p] = o0;
+    }
+}
+
+// Writes survivors in candidate (= key) order: keys and float(alpha / scale).
+// grid = (NCH, B)
+__global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
+    __shared__ uint32_t sm_off[CH];
+    __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
+    const int p = blockIdx.y, c = blockIdx.x;
+    const uint64_t pc = (uint64_t)p * a.NCH + c;
+    const uint64_t cb = a.chunk_cand_off[pc];
+    const uint32_t ncand = (uint32_t)(a.chunk_cand_off[pc + 1] - cb);
+    if (a.chunk_surv[pc] == 0) return;
+    const uint64_t q0 = (uint64_t)c * CH;
+    const uint32_t nq = (uint32_t)min((uint64_t)CH, a.T1 - q0);
+    const uint32_t *coff = a.coff + (uint64_t)p * a.T1;
+    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+    uint32_t local0 = coff[q0];
+    for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
+    __syncthreads();
+    const double scale = a.scale[p];
+    const float vm1 = __double2float_rn(__ddiv_rn(-1.0, scale));
+    // destination: proteome base in the caller's arena + offset within proteome
+    const uint64_t pbase = a.chunk_out_off[(uint64_t)p * a.NCH];
+    uint64_t dst = a.dst_base[p] + (a.chunk_out_off[pc] - pbase);
+    const uint64_t dst_end = a.dst_base[p] + a.dst_cap[p];
+    const uint32_t A = a.A;
+    for (uint32_t base = 0; base < ncand; base += CHUNK_THREADS) {
+        const uint32_t u = base + threadIdx.x;
+        uint32_t bits = 0;
+        uint32_t key = 0;
+        if (u < ncand && cb + u < a.cand_cap) {
+            bits = a.c0a[cb + u];
+            if (bits) {
+                uint32_t ql, r;
+                locate(sm_off, nq, u, ql, r);
+                const uint64_t q = q0 + ql;
+                const uint32_t m = (uint32_t)(q % a.T2);
+                key = (uint32_t)(q * A + nth_set_bit(mk[m], r));
+            }
+        }
+        uint64_t tot;
+        uint64_t rank = block_excl_scan_u64<CHUNK_THREADS>(bits ? 1u : 0u, sw, &tot);
+        if (bits) {
+            const uint64_t o = dst + rank;
+            if (o < dst_end) {
+                const float f = __uint_as_float(bits);
+                a.out_keys[o] = key;
+                a.out_vals[o] = (f == -1.0f) ? vm1 : __double2float_rn(__ddiv_rn((double)f, scale));
+            }
+        }
+        dst += tot;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+int build_geometry(int alpha, int k, BuildGeometry *g) {
+    if (alpha != ALPHA_PROTEIN && alpha != ALPHA_DNA) return -1;
+    if (k < 3 || k > 10) return -1;
+    const uint64_t A = alphabet_size(alpha);
+    if (ipow64(A, k) > 0xffffffffull) return -2;  // keys must fit uint32
+    g->alpha = alpha;
+    g->k = k;
+    g->A = (uint32_t)A;
+    g->T1 = ipow64(A, k - 1);
+    g->T2 = ipow64(A, k - 2);
+    g->NCH = div_up(g->T1, CH);
+    return 0;
+}
+
+size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
+    const uint64_t nc = (uint64_t)B * g.NCH;
+    size_t s = 0;
+    s += scratch_bytes<uint32_t>(g.T1 * B);        // c1
+    s += scratch_bytes<uint32_t>(g.T1 * B);        // coff
+    s += scratch_bytes<uint32_t>(g.T2 * B);        // c2
+    s += scratch_bytes<uint32_t>(g.T2 * B);        // mask
+    s += scratch_bytes<uint32_t>(4 * (uint64_t)B); // tot
+    s += scratch_bytes<uint64_t>(B + 1);           // seq_off (single-proteome path)
+    s += scratch_bytes<uint64_t>(B + 1);           // tile_base
+    s += scratch_bytes<uint32_t>(nc);              // chunk_cand
+    s += scratch_bytes<uint64_t>(nc + 1);          // chunk_cand_off
+    s += scratch_bytes<uint32_t>(nc);              // chunk_surv
+    s += scratch_bytes<uint64_t>(nc + 1);          // chunk_out_off
+    s += scratch_bytes<uint32_t>(nc);              // chunk_m1
+    s += scratch_bytes<double>(nc);                // chunk_nhi
+    s += scratch_bytes<double>(nc);                // chunk_nlo
+    s += scratch_bytes<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);  // scan temp
+    s += scratch_bytes<double>(B);                 // norm
+    s += scratch_bytes<double>(B);                 // scale
+    s += scratch_bytes<uint64_t>(B);               // nnz
+    s += scratch_bytes<uint64_t>(B);               // out_base
+    s += scratch_bytes<uint64_t>(B);               // dst_base
+    s += scratch_bytes<uint64_t>(B);               // dst_cap
+    s += scratch_bytes<uint32_t>(4);               // status
+    s += scratch_bytes<uint32_t>(cand_cap);        // c0a
+    return s;
+}
+
+cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *scratch,
+                        size_t scratch_size, BuildArgs *a) {
+    Scratch sc(scratch, scratch_size);
+    const uint64_t nc = (uint64_t)B * g.NCH;
+    BuildArgs &r = *a;
+    r.alpha = g.alpha; r.k = g.k; r.A = g.A; r.T1 = g.T1; r.T2 = g.T2; r.NCH = g.NCH; r.B = B;
+    r.c1 = sc.take<uint32_t>(g.T1 * B);
+    r.coff = sc.take<uint32_t>(g.T1 * B);
+    r.c2 = sc.take<uint32_t>(g.T2 * B);
+    r.mask = sc.take<uint32_t>(g.T2 * B);
+    r.tot = sc.take<uint32_t>(4 * (uint64_t)B);
+    r.seq_off_store = sc.take<uint64_t>(B + 1);
+    r.tile_base = sc.take<uint64_t>(B + 1);
+    r.chunk_cand = sc.take<uint32_t>(nc);
+    r.chunk_cand_off = sc.take<uint64_t>(nc + 1);
+    r.chunk_surv = sc.take<uint32_t>(nc);
+    r.chunk_out_off = sc.take<uint64_t>(nc + 1);
+    r.chunk_m1 = sc.take<uint32_t>(nc);
+    r.chunk_nhi = sc.take<double>(nc);
+    r.chunk_nlo = sc.take<double>(nc);
+    r.scan_tmp = sc.take<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);
+    r.norm = sc.take<double>(B);
+    r.scale = sc.take<double>(B);
+    r.nnz = sc.take<uint64_t>(B);
+    r.out_base = sc.take<uint64_t>(B);
+    r.dst_base = sc.take<uint64_t>(B);
+    r.dst_cap = sc.take<uint64_t>(B);
+    r.status = sc.take<uint32_t>(4);
+    r.c0a = sc.take<uint32_t>(cand_cap);
+    r.cand_cap = cand_cap;
+    if (!r.c0a) return cudaErrorInvalidValue;  // scratch too small
+    return cudaSuccess;
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 152;
+    }
+    return n;
+}
+
+// Phase 1: everything up to per-proteome nnz (no host sync inside).
+cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
+    const uint64_t nc = (uint64_t)a.B * a.NCH;
+    // dense tables c1 | coff | c2 | mask | tot are contiguous in scratch: zero what needs it
+    PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1 * a.B, st));
+    PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
+    PHYLO_CHECK(cudaMemsetAsync(a.mask, 0, sizeof(uint32_t) * a.T2 * a.B, st));
+    PHYLO_CHECK(cudaMemsetAsync(a.tot, 0, sizeof(uint32_t) * 4 * a.B, st));
+    PHYLO_CHECK(cudaMemsetAsync(a.status, 0, sizeof(uint32_t) * 4, st));
+    k_prep<<<1, 32, 0, st>>>(a.B, a.seq_off, a.tile_base);
+    const int grid_seq = sm_count() * 8;
+    k_count<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
+    dim3 gch((unsigned)a.NCH, (unsigned)a.B);
+    k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
+    PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
+    k_cand_offsets<<<gch, CHUNK_THREADS, 0, st>>>(a);
+    k_c0_zero<<<sm_count() * 4, 256, 0, st>>>(a);
+    k_c0_scatter<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
+    k_alpha<<<gch, CHUNK_THREADS, 0, st>>>(a);
+    PHYLO_CHECK(scan_u32_to_u64(a.chunk_surv, nc, a.chunk_out_off, a.scan_tmp, st));
+    k_norm<<<a.B, 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Phase 2: write survivors to out_keys/out_vals at dst_base[p] (capacity dst_cap[p]).
+cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
+    dim3 gch((unsigned)a.NCH, (unsigned)a.B);
+    k_compact<<<gch, CHUNK_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Kernel counting per launch of build_plan + build_emit (for launch accounting).
+// Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_cand_count,
+// scan (3), k_cand_offsets, k_c0_zero, k_c0_scatter, k_alpha, scan (3), k_norm;
+// emit k_arena_offsets, k_compact, k_arena_pad.  (Five memsets are not counted.)
+int build_launches_per_batch() { return 14 + 3; }
+
+}  // namespace phylo

@@ -1,0 +1,413 @@
+"""Batched composition-vector construction and the all-pair engine.
+
+This is the batched counterpart of the reference's per-item pipeline
+(DeviceWorker.loadInput -> preprocessInputGPU for every proteome, then
+correlateGPU for every pair; rocket/scheduler/DeviceWorker.java:118-323):
+
+* :class:`BatchBuilder` builds many proteomes per launch sequence into one
+  device arena (keys | values | offsets), vectors padded to 4 entries so the
+  pair kernel can read them with 16-byte loads.
+* :class:`PairEngine` compares every pair of an arena (or a rectangle of row
+  and column vectors) with the window-tiled kernel of csrc/allpairs.cu.  The
+  planner sorts vectors by size, cuts the pair matrix into 16 x 256 tiles and
+  the key space into segments, estimates each item's cost and hands items out
+  longest first.
+
+All device memory is held in torch tensors; every kernel is this project's
+own (libphylogenetics.so).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native
+from ._native import check
+
+AP_TI = 16
+AP_TJ = 256
+NSYM = {"protein": 21, "DNA": 4}
+
+
+def _p(t: torch.Tensor) -> int:
+    return int(t.data_ptr())
+
+
+def _stream_handle(stream: Optional[torch.cuda.Stream]) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def key_limit(alphabet: str, k: int) -> int:
+    return NSYM[alphabet] ** k
+
+
+# --------------------------------------------------------------------------
+# arena
+# --------------------------------------------------------------------------
+
+@dataclass
+class Arena:
+    """Device-resident composition vectors: vector v is keys/values[off[v] : off[v] + nnz[v]]."""
+    alphabet: str
+    k: int
+    keys: torch.Tensor          # int32 (uint32 bit patterns)
+    values: torch.Tensor        # float32
+    vec_off: torch.Tensor       # int64 [capacity_vectors + 1]
+    nnz: np.ndarray             # int64 [n]
+    off: np.ndarray             # int64 [n + 1] host copy of vec_off
+    norms: np.ndarray           # float64 [n]
+    n: int = 0
+    roff: Optional[torch.Tensor] = None
+    wshift: int = 0
+    R: int = 0
+    indexed: int = 0            # vectors covered by roff
+
+    @property
+    def used(self) -> int:
+        return int(self.off[self.n])
+
+    def reset(self) -> "Arena":
+        """Forgets the vectors but keeps the device buffers for reuse."""
+        self.n = 0
+        self.nnz = np.zeros(0, np.int64)
+        self.off = np.zeros(1, np.int64)
+        self.norms = np.zeros(0, np.float64)
+        self.indexed = 0
+        return self
+
+    def vector(self, v: int):
+        o, m = int(self.off[v]), int(self.nnz[v])
+        return self.keys[o:o + m], self.values[o:o + m]
+
+    def host_vector(self, v: int):
+        k, x = self.vector(v)
+        return k.cpu().numpy().view(np.uint32), x.cpu().numpy()
+
+
+def _grow(t: torch.Tensor, n: int) -> torch.Tensor:
+    if t.numel() >= n:
+        return t
+    new = torch.empty(int(n), dtype=t.dtype, device=t.device)
+    new[:t.numel()].copy_(t)
+    return new
+
+
+class BatchBuilder:
+    """Builds composition vectors of many proteomes into an :class:`Arena`."""
+
+    def __init__(self, alphabet: str = "protein", k: int = 6, device=None, max_batch: int = 64):
+        self.alphabet = alphabet
+        self.k = k
+        self.device = torch.device(device if device is not None else "cuda")
+        self.max_batch = max_batch
+        self.L = _native.load()
+        self._scratch = None
+        self.launches = 0
+
+    def _scratch_for(self, B: int, cand_cap: int) -> torch.Tensor:
+        n = int(self.L.phyloBuildBatchScratch(self.alphabet.encode(), self.k, B, cand_cap))
+        if n < 0:
+            raise ValueError(f"invalid build geometry: alphabet={self.alphabet} k={self.k}")
+        if self._scratch is None or self._scratch.numel() < n:
+            self._scratch = torch.empty(n, dtype=torch.uint8, device=self.device)
+        return self._scratch
+
+    def new_arena(self, capacity_entries: int, capacity_vectors: int) -> Arena:
+        keys = torch.empty(max(int(capacity_entries), 4), dtype=torch.int32, device=self.device)
+        vals = torch.empty(max(int(capacity_entries), 4), dtype=torch.float32, device=self.device)
+        off = torch.zeros(capacity_vectors + 1, dtype=torch.int64, device=self.device)
+        return Arena(self.alphabet, self.k, keys, vals, off, np.zeros(0, np.int64),
+                     np.zeros(1, np.int64), np.zeros(0, np.float64))
+
+    def build(self, seq: torch.Tensor, seq_off: np.ndarray, arena: Optional[Arena] = None,
+              stream: Optional[torch.cuda.Stream] = None) -> Arena:
+        """Builds the proteomes seq[seq_off[i]:seq_off[i+1]] (seq on the device) and
+        appends them to ``arena`` (a new one if None)."""
+        seq_off = np.asarray(seq_off, np.int64)
+        n = len(seq_off) - 1
+        lens = np.diff(seq_off)
+        if arena is None:
+            arena = self.new_arena(int(np.sum(8 * lens + 64)) + 1024, n)
+        if arena.vec_off.numel() < arena.n + n + 1:
+            arena.vec_off = _grow(arena.vec_off, arena.n + n + 1)
+        s_obj = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(s_obj):
+            self._build_into(arena, seq, seq_off, lens, s_obj)
+        return arena
+
+    def _build_into(self, arena: Arena, seq: torch.Tensor, seq_off: np.ndarray, lens: np.ndarray,
+                    stream: torch.cuda.Stream) -> None:
+        n = len(seq_off) - 1
+        st = int(stream.cuda_stream)
+        d_seq_off_all = torch.from_numpy(seq_off).to(self.device, non_blocking=False)
+        first = 0
+        while first < n:
+            B = min(self.max_batch, n - first)
+            sl = slice(first, first + B)
+            lens_b = lens[sl]
+            cand = int(np.sum(np.minimum(8 * lens_b + 65536, key_limit(self.alphabet, self.k))))
+            # offsets of this sub-batch relative to its first proteome
+            base = int(seq_off[first])
+            d_off = d_seq_off_all[first:first + B + 1] - base
+            d_seq = seq[base:int(seq_off[first + B])]
+            nnz = np.zeros(B, np.int64)
+            total_cand = np.zeros(1, np.int64)
+            for attempt in range(2):
+                scr = self._scratch_for(B, cand)
+                rc = self.L.phyloBuildBatchPlan(
+                    st, _p(scr), scr.numel(), self.alphabet.encode(), self.k, B,
+                    _p(d_seq) if d_seq.numel() else _p(seq), _p(d_off), cand,
+                    nnz.ctypes.data, total_cand.ctypes.data)
+                if rc == 2 and attempt == 0:  # capacity: retry with the exact count
+                    cand = int(total_cand[0])
+                    continue
+                check(rc)
+                break
+            self.launches += int(self.L.phyloBuildLaunchesPerBatch())
+            norms = np.zeros(B, np.float64)
+            check(self.L.phyloBuildBatchNorms(st, _p(scr), scr.numel(), self.alphabet.encode(),
+                                              self.k, B, cand, norms.ctypes.data))
+            padded = (nnz + 3) // 4 * 4
+            need = arena.used + int(padded.sum()) + 4
+            if arena.keys.numel() < need:
+                cap = int(max(need, arena.keys.numel() * 1.5))
+                arena.keys = _grow(arena.keys, cap)
+                arena.values = _grow(arena.values, cap)
+            check(self.L.phyloBuildBatchEmit(
+                st, _p(scr), scr.numel(), self.alphabet.encode(), self.k, B, cand,
+                _p(arena.keys), _p(arena.values), _p(arena.vec_off[arena.n:]), arena.used))
+            arena.nnz = np.concatenate([arena.nnz, nnz])
+            arena.norms = np.concatenate([arena.norms, norms])
+            new_off = arena.used + np.concatenate([[0], np.cumsum(padded)])
+            arena.off = np.concatenate([arena.off[:arena.n], new_off])
+            arena.n += B
+            first += B
+
+
+def upload_proteomes(data: np.ndarray, device=None, pinned: Optional[torch.Tensor] = None,
+                     non_blocking: bool = True) -> torch.Tensor:
+    """Host residue bytes -> device tensor (through pinned memory)."""
+    h = torch.from_numpy(np.ascontiguousarray(data))
+    if pinned is None:
+        pinned = h.pin_memory()
+    else:
+        pinned[:h.numel()].copy_(h)
+    d = torch.empty(h.numel(), dtype=torch.uint8, device=device or "cuda")
+    d.copy_(pinned[:h.numel()], non_blocking=non_blocking)
+    return d
+
+
+# --------------------------------------------------------------------------
+# pair engine
+# --------------------------------------------------------------------------
+
+@dataclass
+class PairPlan:
+    rowids: torch.Tensor       # int32 device
+    colids: torch.Tensor
+    tiles: torch.Tensor        # int32 device [ntiles, 4]
+    items: torch.Tensor        # int32 device [nitems, 8]
+    ntiles: int
+    nitems: int
+    S: int
+    upper: bool
+    mirror: bool
+    ldc: int
+    est: np.ndarray            # estimated cost per item (launch order)
+    est_product: np.ndarray    # nnz-product estimate per item
+    pairs: int                 # valid pairs covered
+    host_items: np.ndarray = field(default=None)
+
+
+@dataclass
+class EngineConfig:
+    wshift: int = 10
+    fold: int = 16
+    items_per_cta: int = 4
+    min_windows_per_item: int = 64
+
+
+class PairEngine:
+    def __init__(self, arena: Arena, config: Optional[EngineConfig] = None):
+        self.arena = arena
+        self.cfg = config or EngineConfig()
+        self.L = _native.load()
+        self.device = arena.keys.device
+        ctas = ctypes.c_int(0)
+        check(self.L.phyloPairsPrepare(self.cfg.wshift, ctypes.byref(ctas)))
+        self.ctas_per_sm = max(1, ctas.value)
+        props = torch.cuda.get_device_properties(self.device)
+        self.sms = props.multi_processor_count
+        self.grid = self.sms * self.ctas_per_sm
+        self.counter = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.part = None
+        self.launches = 0
+        self.cmp_scratch = None
+
+    # -- window index ------------------------------------------------------
+    def ensure_index(self, stream=None) -> None:
+        """Builds (or extends to newly appended vectors) the window index."""
+        a = self.arena
+        W = 1 << self.cfg.wshift
+        R = (key_limit(a.alphabet, a.k) + W - 1) // W
+        if a.roff is None or a.wshift != self.cfg.wshift:
+            a.roff = torch.empty((max(a.n, 1), R + 1), dtype=torch.int32, device=self.device)
+            a.wshift, a.R, a.indexed = self.cfg.wshift, R, 0
+        if a.roff.shape[0] < a.n:
+            new = torch.empty((int(a.n * 1.5) + 1, R + 1), dtype=torch.int32, device=self.device)
+            new[:a.roff.shape[0]].copy_(a.roff)
+            a.roff = new
+        if a.indexed < a.n:
+            check(self.L.phyloWindowIndex(
+                _stream_handle(stream), _p(a.keys), _p(a.vec_off[a.indexed:]), a.n - a.indexed,
+                self.cfg.wshift, R, _p(a.roff[a.indexed])))
+            self.launches += 1
+            a.indexed = a.n
+
+    # -- planning ------------------------------------------------------------
+    def _segments(self, ntiles: int) -> int:
+        target = self.cfg.items_per_cta * self.grid
+        S = max(1, math.ceil(target / max(ntiles, 1)))
+        return int(max(1, min(S, self.arena.R // self.cfg.min_windows_per_item)))
+
+    def _finish_plan(self, rowids, colids, tiles, upper, mirror, ldc, pairs) -> PairPlan:
+        a = self.arena
+        ntiles = len(tiles)
+        S = self._segments(ntiles)
+        R = a.R
+        nnz = a.nnz
+        items = np.zeros((ntiles * S, 8), np.int64)
+        est = np.zeros(ntiles * S)
+        estp = np.zeros(ntiles * S)
+        for t, (r0, nr, c0, nc) in enumerate(tiles):
+            rn = nnz[rowids[r0:r0 + nr]]
+            cn = nnz[colids[c0:c0 + nc]]
+            # linear model: 16 products per column entry + row scatter/clear
+            # + a fixed cost per window
+            e_tile = AP_TI * cn.sum() + 2.0 * rn.sum() + 64.0 * R
+            # nnz-product estimate: sum over the tile's pairs of sqrt(nnz_i * nnz_j)
+            e_prod = float(np.sqrt(np.outer(rn, cn)).sum())
+            for s in range(S):
+                i = t * S + s
+                items[i] = (r0, nr, c0, nc, s * R // S, (s + 1) * R // S, i, t)
+                est[i] = e_tile / S
+                estp[i] = e_prod / S
+        order = np.argsort(-est, kind="stable")
+        items = items[order]
+        est = est[order]
+        estp = estp[order]
+        dev = self.device
+        return PairPlan(
+            rowids=torch.from_numpy(np.asarray(rowids, np.int64).astype(np.int32)).to(dev),
+            colids=torch.from_numpy(np.asarray(colids, np.int64).astype(np.int32)).to(dev),
+            tiles=torch.from_numpy(np.asarray(tiles, np.int32).reshape(-1, 4)).to(dev),
+            items=torch.from_numpy(items.astype(np.int32)).to(dev),
+            ntiles=ntiles, nitems=len(items), S=S, upper=upper, mirror=mirror, ldc=ldc,
+            est=est, est_product=estp, pairs=pairs, host_items=items)
+
+    def plan_triangle(self, ids: Optional[Sequence[int]] = None, ldc: Optional[int] = None) -> PairPlan:
+        """All pairs i < j among ``ids`` (default: every vector of the arena)."""
+        a = self.arena
+        ids = np.arange(a.n) if ids is None else np.asarray(ids, np.int64)
+        order = np.argsort(-a.nnz[ids], kind="stable")
+        perm = ids[order]
+        N = len(perm)
+        tiles = []
+        for r0 in range(0, N, AP_TI):
+            nr = min(AP_TI, N - r0)
+            c = r0 + 1
+            while c < N:
+                nc = min(AP_TJ, N - c)
+                tiles.append((r0, nr, c, nc))
+                c += nc
+        return self._finish_plan(perm, perm, tiles, True, True, ldc or a.n, N * (N - 1) // 2)
+
+    def plan_rect(self, row_ids: Sequence[int], col_ids: Sequence[int], ldc: int) -> PairPlan:
+        """Every (row, column) pair; out[row_id * ldc + col_id]."""
+        a = self.arena
+        rows = np.asarray(row_ids, np.int64)
+        cols = np.asarray(col_ids, np.int64)
+        rows = rows[np.argsort(-a.nnz[rows], kind="stable")]
+        cols = cols[np.argsort(-a.nnz[cols], kind="stable")]
+        tiles = []
+        for r0 in range(0, len(rows), AP_TI):
+            nr = min(AP_TI, len(rows) - r0)
+            for c0 in range(0, len(cols), AP_TJ):
+                tiles.append((r0, nr, c0, min(AP_TJ, len(cols) - c0)))
+        return self._finish_plan(rows, cols, tiles, False, False, ldc, len(rows) * len(cols))
+
+    # -- execution -------------------------------------------------------------
+    def _parts(self, plan: PairPlan) -> torch.Tensor:
+        need = plan.ntiles * plan.S * AP_TI * AP_TJ * 2
+        if self.part is None or self.part.numel() < need:
+            self.part = torch.empty(need, dtype=torch.float32, device=self.device)
+        return self.part
+
+    def run(self, plan: PairPlan, out: torch.Tensor, stream=None, item_cycles: torch.Tensor = None,
+            diagonal: bool = True, events=None) -> None:
+        """Writes C of every planned pair into ``out`` (float64, row-major, ldc).
+        ``events`` = (start, end) CUDA events recorded around the pair kernel."""
+        a = self.arena
+        s_obj = stream if stream is not None else torch.cuda.current_stream(self.device)
+        st = int(s_obj.cuda_stream)
+        part = self._parts(plan)
+        with torch.cuda.stream(s_obj):
+            self.counter.zero_()
+        if events is not None:
+            events[0].record(s_obj)
+        check(self.L.phyloPairsLaunch(
+            st, _p(a.keys), _p(a.values), _p(a.vec_off), _p(a.roff), a.R, self.cfg.wshift,
+            _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems, _p(self.counter),
+            _p(part), self.cfg.fold, _p(item_cycles) if item_cycles is not None else 0,
+            self.grid))
+        if events is not None:
+            events[1].record(s_obj)
+        check(self.L.phyloPairsReduce(
+            st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, _p(plan.rowids), _p(plan.colids),
+            _p(out), plan.ldc, int(plan.upper), int(plan.mirror)))
+        self.launches += 3  # counter fill, pair kernel, reduction
+        if diagonal and plan.upper:
+            check(self.L.phyloSelfDot(st, _p(a.values), _p(a.vec_off), a.n, _p(out), plan.ldc))
+            self.launches += 1
+        self._fix_nonfinite(plan, out, s_obj)
+
+    def _fix_nonfinite(self, plan: PairPlan, out: torch.Tensor, stream) -> None:
+        """Vectors whose values are NaN/inf: recompute their pairs with the
+        merge-path kernel, which only multiplies values of shared keys (as the
+        reference does)."""
+        a = self.arena
+        bad = np.flatnonzero(~np.isfinite(a.norms[:a.n]))
+        if len(bad) == 0:
+            return
+        st = _stream_handle(stream)
+        maxn = int(a.nnz.max())
+        if self.cmp_scratch is None:
+            n = int(self.L.estimateScratchMemory(a.alphabet.encode(), 3, maxn))
+            self.cmp_scratch = torch.empty(n, dtype=torch.uint8, device=self.device)
+        rows = plan.rowids.cpu().numpy()
+        cols = plan.colids.cpu().numpy()
+        ks, vs = a.keys, a.values
+        for r in rows:
+            for c in cols:
+                if r == c or not (r in bad or c in bad):
+                    continue
+                if plan.upper and not (np.flatnonzero(rows == r)[0] < np.flatnonzero(cols == c)[0]):
+                    continue
+                o = out.view(-1)[int(r) * plan.ldc + int(c):]
+                check(self.L.phyloComparePairAsync(
+                    st, _p(self.cmp_scratch), self.cmp_scratch.numel(), _p(ks[a.off[r]:]),
+                    _p(vs[a.off[r]:]), int(a.nnz[r]), _p(ks[a.off[c]:]), _p(vs[a.off[c]:]),
+                    int(a.nnz[c]), _p(o)))
+                if plan.mirror:
+                    out.view(-1)[int(c) * plan.ldc + int(r)] = out.view(-1)[int(r) * plan.ldc + int(c)]
+
+
+def distances(c: torch.Tensor) -> torch.Tensor:
+    """D = (1 - C) / 2."""
+    return (1.0 - c) * 0.5

@@ -1,0 +1,120 @@
+"""Composition-vector construction on the device vs the oracle's restatement of
+native.cu's rule: keys and counts bit-exact, values within 1 ulp (the norm is an
+exactly rounded sum on both sides, so they are normally identical)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from rocket_gb300 import _native, synth
+from rocket_gb300.engine import BatchBuilder
+
+from gpu_helpers import build_gpu, ulp_diff, to_device_bytes
+
+pytestmark = pytest.mark.gpu
+
+
+def check_against_oracle(seq, k, alphabet="protein", max_size=None):
+    n, keys, vals = build_gpu(seq, k, alphabet, max_size)
+    r = O.cv_native(seq, k, alphabet)
+    assert n == len(r["keys"])
+    assert np.array_equal(keys[:n], r["keys"])
+    assert ulp_diff(vals[:n], r["values"]) <= 1
+    # padding (native.cu:473-474)
+    assert np.all(keys[n:] == 0xFFFFFFFF) and np.all(vals[n:] == 0)
+    return n
+
+
+@pytest.mark.parametrize("seq,k,expect", [
+    (b"ACACA", 3, 2), (b"AAAAA", 3, 0), (b"ACA\nCC", 3, 5), (b"AC\nCA", 3, 2),
+    (b"", 3, 0), (b"A", 3, 0), (b"AC", 3, 0), (b"ACDEFGHIKLMNPQRSTVWYX", 6, None),
+    (b"ACDE\nFGHI", 4, None), (b"XYXYX", 3, None),
+])
+def test_known_answers(seq, k, expect):
+    n = check_against_oracle(seq, k)
+    if expect is not None:
+        assert n == expect
+
+
+@pytest.mark.parametrize("k", [3, 4, 5, 6])
+def test_bindings_sweep_protein(k):
+    # the sweep of BindingsTest.testBuildVectors (n x seeds, :99-112)
+    for n in (10, 100, 1000, 10000):
+        for seed in range(5):
+            check_against_oracle(O.bindings_input(seed, n), k)
+
+
+@pytest.mark.parametrize("k", [3, 5, 7, 9])
+def test_bindings_sweep_dna(k):
+    for n in (10, 100, 1000, 10000):
+        for seed in range(5):
+            check_against_oracle(O.bindings_input(seed, n, "DNA"), k, "DNA")
+
+
+def test_dna_k10():
+    check_against_oracle(O.bindings_input(9, 50000, "DNA"), 10, "DNA")
+
+
+@pytest.mark.parametrize("k", [5, 6, 7])
+def test_synthetic_proteome(k):
+    p = synth.workload("uniform256", n=2, scale=0.2)
+    check_against_oracle(p.get(1), k)
+
+
+def test_full_size_proteome_k6():
+    p = synth.workload("uniform256", n=1)
+    n = check_against_oracle(p.get(0), 6)
+    assert n > 10 ** 6
+
+
+def test_exact_capacity_and_overflow():
+    s = O.bindings_input(2, 3000)
+    r = O.cv_native(s, 4)
+    n = len(r["keys"])
+    assert check_against_oracle(s, 4, max_size=n) == n  # size == max: no padding
+    with pytest.raises(_native.CudaException) as e:
+        build_gpu(s, 4, max_size=n - 1)
+    assert e.value.code == 999
+
+
+@pytest.mark.parametrize("alphabet,k", [("protein", 2), ("protein", 11), ("protein", 8),
+                                        ("rna", 5), ("DNA", 2)])
+def test_argument_errors(alphabet, k):
+    from rocket_gb300.bindings import Bindings
+    d_in = to_device_bytes(b"ACDEFGHIK")
+    keys = torch.empty(64, dtype=torch.int32, device="cuda")
+    vals = torch.empty(64, dtype=torch.float32, device="cuda")
+    scr = torch.empty(1 << 20, dtype=torch.uint8, device="cuda")
+    size = np.zeros(1, np.int32)
+    rc = Bindings.INSTANCE.buildCompositionVector(
+        torch.cuda.current_stream().cuda_stream, scr.data_ptr(), scr.numel(), alphabet, k,
+        d_in.data_ptr(), 9, keys.data_ptr(), vals.data_ptr(), size, 64)
+    assert rc == 999
+
+
+def test_batched_build_equals_single_and_counts():
+    p = synth.workload("uneven1024", n=6, scale=0.05)
+    d = torch.from_numpy(p.data).cuda()
+    b = BatchBuilder("protein", 6, max_batch=4)  # two sub-batches
+    arena = b.build(d, p.offsets)
+    torch.cuda.synchronize()
+    assert arena.n == 6
+    for i in range(6):
+        r = O.cv_native(p.get(i), 6)
+        k, v = arena.host_vector(i)
+        assert np.array_equal(k, r["keys"])
+        assert ulp_diff(v, r["values"]) <= 1
+        assert arena.off[i] % 4 == 0
+        assert abs(arena.norms[i] - r["norm"]) <= 1e-12 * r["norm"]
+    # count tables of the last plan (proteomes 4, 5)
+    L = _native.load()
+    scr = b._scratch
+    k1 = np.zeros(21 ** 5, np.uint32)
+    k2 = np.zeros(21 ** 4, np.uint32)
+    tot = np.zeros(3, np.uint32)
+    cand = int(np.sum(np.minimum(8 * p.lengths()[4:] + 65536, 21 ** 6)))
+    _native.check(L.phyloBuildBatchCounts(torch.cuda.current_stream().cuda_stream,
+                                          scr.data_ptr(), scr.numel(), b"protein", 6, 2, cand, 1,
+                                          k1.ctypes.data, k2.ctypes.data, tot.ctypes.data))
+    e1, e2, et = O.count_tables(p.get(5), 6)
+    assert np.array_equal(k1, e1) and np.array_equal(k2, e2) and tuple(tot) == et
