@@ -215,7 +215,7 @@ def run_ours(args):
     from rocket_gb300 import synth
     from rocket_gb300.engine import BatchBuilder, EngineConfig, PairEngine
 
-    wl = synth.workload(WORKLOAD)
+    wl = synth.workload(WORKLOAD, n=args.proteomes)
     N = len(wl)
     n_pairs = N * (N - 1) // 2
     stream = torch.cuda.current_stream(dev)
@@ -235,16 +235,21 @@ def run_ours(args):
 
     def step(record_kernel=False):
         nonlocal arena, engine
+        ev = None
+        if record_kernel:
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            ev[2].record(stream)
         arena = builder.build(seq, wl.offsets, arena=arena.reset() if arena is not None else None,
                               stream=stream)
         if engine is None:
             engine = PairEngine(arena, cfg)
         engine.arena = arena
-        engine.ensure_index(stream)
-        plan = engine.plan_triangle()
-        ev = None
         if record_kernel:
-            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[3].record(stream)
+        engine.ensure_index(stream)
+        if record_kernel:
+            ev[4].record(stream)
+        plan = engine.plan_triangle()
         engine.run(plan, out, stream=stream, events=ev)
         state["plan"] = plan
         return ev
@@ -263,6 +268,7 @@ def run_ours(args):
     # timed device-resident steps
     launches0 = builder.launches + engine.launches
     step_ms = []
+    phase_ms = []
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -278,6 +284,8 @@ def run_ours(args):
             torch.cuda.synchronize()
             step_ms.append(e0.elapsed_time(e1))
             kernel_ms.append(ev[0].elapsed_time(ev[1]))
+            phase_ms.append((ev[2].elapsed_time(ev[3]), ev[3].elapsed_time(ev[4]),
+                             ev[4].elapsed_time(ev[0]), ev[1].elapsed_time(e1)))
     launches = (builder.launches + engine.launches - launches0) // args.steps
     total_s = sum(step_ms) / 1000.0
     total_s = _barrier_max(total_s, world)
@@ -318,7 +326,12 @@ def run_ours(args):
             "window_shift": args.wshift, "fold": args.fold, "items": plan.nitems,
             "segments": plan.S,
         },
-        "breakdown_ms": {"pair_kernel": k_ms, "step": float(np.mean(step_ms))},
+        "breakdown_ms": {"build": float(np.mean([p[0] for p in phase_ms])),
+                         "window_index": float(np.mean([p[1] for p in phase_ms])),
+                         "plan_and_launch_gap": float(np.mean([p[2] for p in phase_ms])),
+                         "pair_kernel": k_ms,
+                         "reduce_and_self": float(np.mean([p[3] for p in phase_ms])),
+                         "step": float(np.mean(step_ms))},
         "roofline": {
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic,
@@ -354,6 +367,8 @@ def main():
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--proteomes", type=int, default=None,
+                    help="use only the first N proteomes (small profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -27,7 +27,7 @@ namespace phylo {
 constexpr int CMP_THREADS = 256;
 constexpr int CMP_IPT = 16;
 constexpr int CMP_TILE = CMP_THREADS * CMP_IPT;  // merged elements per tile
-constexpr int CMP_BUF = CMP_TILE + 16;           // entries per stage per type (A part + B part)
+constexpr int CMP_BUF = CMP_TILE + 20;           // entries per stage per type (A + B + look-ahead)
 constexpr int CMP_MAX_CTAS = 1024;
 
 struct CmpState {
@@ -82,11 +82,12 @@ __global__ void k_partition(const uint32_t *__restrict__ A, uint32_t na,
 struct Stage {
     uint32_t ka_off, va_off, kb_off, vb_off;  // element offsets of the first wanted entry
     uint32_t na, nb;
+    uint32_t nbx;  // nb plus one look-ahead right element when the right list continues
 };
 
 // Issues the bulk copies of tile `t` into buffer `buf`; returns the stage layout.
 __device__ __forceinline__ Stage issue_tile(uint32_t t, const uint32_t *splits, uint64_t total,
-                                            const uint32_t *Ak, const float *Av,
+                                            uint32_t nb_total, const uint32_t *Ak, const float *Av,
                                             const uint32_t *Bk, const float *Bv, uint32_t *sk,
                                             float *sv, uint64_t *bar, bool issue) {
     Stage s;
@@ -96,17 +97,22 @@ __device__ __forceinline__ Stage issue_tile(uint32_t t, const uint32_t *splits, 
     const uint32_t j0 = (uint32_t)(d0 - i0), j1 = (uint32_t)(d1 - i1);
     s.na = i1 - i0;
     s.nb = j1 - j0;
+    // A match whose left element ends this tile can have its equal right element
+    // start the next one (ties go left), so one right element past the tile is
+    // copied as look-ahead.
+    const uint32_t j1x = j1 < nb_total ? j1 + 1 : j1;
+    s.nbx = j1x - j0;
     // widened byte ranges
     const uintptr_t ka0 = (uintptr_t)(Ak + i0), ka1 = (uintptr_t)(Ak + i1);
     const uintptr_t va0 = (uintptr_t)(Av + i0), va1 = (uintptr_t)(Av + i1);
-    const uintptr_t kb0 = (uintptr_t)(Bk + j0), kb1 = (uintptr_t)(Bk + j1);
-    const uintptr_t vb0 = (uintptr_t)(Bv + j0), vb1 = (uintptr_t)(Bv + j1);
+    const uintptr_t kb0 = (uintptr_t)(Bk + j0), kb1 = (uintptr_t)(Bk + j1x);
+    const uintptr_t vb0 = (uintptr_t)(Bv + j0), vb1 = (uintptr_t)(Bv + j1x);
     auto lo16 = [](uintptr_t x) { return x & ~(uintptr_t)15; };
     auto hi16 = [](uintptr_t x) { return (x + 15) & ~(uintptr_t)15; };
     const uint32_t bka = s.na ? (uint32_t)(hi16(ka1) - lo16(ka0)) : 0u;
     const uint32_t bva = s.na ? (uint32_t)(hi16(va1) - lo16(va0)) : 0u;
-    const uint32_t bkb = s.nb ? (uint32_t)(hi16(kb1) - lo16(kb0)) : 0u;
-    const uint32_t bvb = s.nb ? (uint32_t)(hi16(vb1) - lo16(vb0)) : 0u;
+    const uint32_t bkb = s.nbx ? (uint32_t)(hi16(kb1) - lo16(kb0)) : 0u;
+    const uint32_t bvb = s.nbx ? (uint32_t)(hi16(vb1) - lo16(vb0)) : 0u;
     // B part starts after the A part (both multiples of 16 bytes)
     s.ka_off = (uint32_t)((ka0 & 15) >> 2);
     s.va_off = (uint32_t)((va0 & 15) >> 2);
@@ -152,13 +158,13 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
     __syncthreads();
 
     FF acc = {0.0f, 0.0f};
-    Stage stg0 = {0, 0, 0, 0, 0, 0}, stg1 = {0, 0, 0, 0, 0, 0};
+    Stage stg0 = {0, 0, 0, 0, 0, 0, 0}, stg1 = {0, 0, 0, 0, 0, 0, 0};
     // prologue: tiles t_begin, t_begin+1
     if (t_begin < t_end)
-        stg0 = issue_tile(t_begin, splits, total, Ak, Av, Bk, Bv, sk[0], sv[0], &bar[0],
+        stg0 = issue_tile(t_begin, splits, total, nb, Ak, Av, Bk, Bv, sk[0], sv[0], &bar[0],
                           threadIdx.x == 0);
     if (t_begin + 1 < t_end)
-        stg1 = issue_tile(t_begin + 1, splits, total, Ak, Av, Bk, Bv, sk[1], sv[1], &bar[1],
+        stg1 = issue_tile(t_begin + 1, splits, total, nb, Ak, Av, Bk, Bv, sk[1], sv[1], &bar[1],
                           threadIdx.x == 0);
     uint32_t fail_at = 0xffffffffu;
     for (uint32_t t = t_begin; t < t_end; t++) {
@@ -190,10 +196,10 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
             uint32_t i = lo, j = d - lo;
             const uint32_t steps = min((uint32_t)CMP_IPT, n - d);
             for (uint32_t it = 0; it < steps; it++) {
-                const bool has_a = i < s.na, has_b = j < s.nb;
-                const uint32_t x = has_a ? ka[i] : 0u, y = has_b ? kb[j] : 0u;
+                const bool has_a = i < s.na, has_b = j < s.nb, has_bx = j < s.nbx;
+                const uint32_t x = has_a ? ka[i] : 0u, y = has_bx ? kb[j] : 0u;
                 const bool take_a = has_a && (!has_b || x <= y);
-                if (take_a && has_b && x == y) {
+                if (take_a && has_bx && x == y) {
                     float p, e;
                     two_prod(va[i], vb[j], p, e);
                     ff_add(acc, p);
@@ -207,7 +213,7 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
         const uint32_t tn = t + 2;
         if (tn < t_end) {
             if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const Stage ns = issue_tile(tn, splits, total, Ak, Av, Bk, Bv, skb, svb, &bar[b],
+            const Stage ns = issue_tile(tn, splits, total, nb, Ak, Av, Bk, Bv, skb, svb, &bar[b],
                                         threadIdx.x == 0);
             if (b) stg1 = ns; else stg0 = ns;
         }
