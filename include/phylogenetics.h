@@ -66,6 +66,32 @@ int compareCompositionVectors(uintptr_t stream, uintptr_t d_temp_storage_ptr, lo
                               uintptr_t d_right_keys_ptr, uintptr_t d_right_values_ptr,
                               int right_size, uintptr_t d_output_ptr);
 
+/*
+ * compareCompositionVectors for callers that cannot allocate device memory.
+ * No counterpart in the reference.
+ *
+ * Some callers have no way to call cudaMalloc: a host runtime that divided all
+ * device memory into fixed cache slots at start-up (Rocket's device cache works
+ * this way) and has no spare buffer for scratch, or a caller whose device
+ * memory is owned by another framework's allocator.  This entry point takes no
+ * scratch argument and allocates nothing: the compare kernels use a fixed-size
+ * array built into the library (about 73 KB, present on every GPU that loads the
+ * library until the process exits).  The caller still passes the inputs and the
+ * output (one double, device memory).
+ *
+ * Limit: left_size + right_size <= 67,108,864 (2^26); larger inputs are refused
+ * with cudaErrorInvalidValue and a message, before any kernel runs.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: calls whose kernels could overlap on the GPU
+ * (other streams, other host threads) must be serialised by the caller.
+ * Synchronous; returns a cudaError_t code like compareCompositionVectors.
+ */
+int compareCompositionVectorsStatic(uintptr_t stream, uintptr_t d_left_keys_ptr,
+                                    uintptr_t d_left_values_ptr, int left_size,
+                                    uintptr_t d_right_keys_ptr, uintptr_t d_right_values_ptr,
+                                    int right_size, uintptr_t d_output_ptr);
+
 /* ---------------------------------------------------------------------------
  * Batched construction (new; the reference builds one proteome per call,
  * driven per item by DeviceWorker.loadInput, DeviceWorker.java:118-157)

@@ -60,6 +60,9 @@ def _declare(L: ctypes.CDLL) -> None:
     L.compareCompositionVectors.argtypes = [c_ptr, c_ptr, c_long, c_ptr, c_ptr, c_int, c_ptr,
                                             c_ptr, c_int, c_ptr]
     L.compareCompositionVectors.restype = c_int
+    L.compareCompositionVectorsStatic.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_ptr, c_ptr, c_int,
+                                                  c_ptr]
+    L.compareCompositionVectorsStatic.restype = c_int
     # batched construction
     L.phyloBuildBatchScratch.argtypes = [c_char_p, c_int, c_int, c_long]
     L.phyloBuildBatchScratch.restype = c_long
@@ -99,7 +102,7 @@ def _declare(L: ctypes.CDLL) -> None:
 # Every symbol that include/phylogenetics.h declares.
 EXPORTED = [
     "estimateScratchMemory", "buildCompositionVector", "compareCompositionVectors",
-    "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchEmit", "phyloBuildBatchNorms",
+    "compareCompositionVectorsStatic", "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchEmit", "phyloBuildBatchNorms",
     "phyloBuildBatchCounts", "phyloBuildLaunchesPerBatch", "phyloWindowIndex",
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsLaunch", "phyloPairsReduce",
     "phyloSelfDot", "phyloComparePairAsync",

@@ -201,6 +201,33 @@ int compareCompositionVectors(uintptr_t stream, uintptr_t d_temp_storage_ptr, lo
     return (int)cudaGetLastError();
 }
 
+// For callers that cannot allocate device memory (see include/phylogenetics.h):
+// compareCompositionVectors on the library's built-in scratch array.
+// Synchronous, like compareCompositionVectors.  No allocation of any kind.
+int compareCompositionVectorsStatic(uintptr_t stream, uintptr_t d_left_keys_ptr,
+                                    uintptr_t d_left_values_ptr, int left_size,
+                                    uintptr_t d_right_keys_ptr, uintptr_t d_right_values_ptr,
+                                    int right_size, uintptr_t d_output_ptr) {
+    if (left_size < 0 || right_size < 0) {
+        fprintf(stderr, "error: negative vector size (%d, %d)\n", left_size, right_size);
+        return (int)cudaErrorInvalidValue;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t *d_status = nullptr;
+    cudaError_t e = compare_launch_static(
+        st, (const uint32_t *)d_left_keys_ptr, (const float *)d_left_values_ptr,
+        (uint32_t)left_size, (const uint32_t *)d_right_keys_ptr,
+        (const float *)d_right_values_ptr, (uint32_t)right_size, (double *)d_output_ptr, &d_status);
+    if (e != cudaSuccess) return (int)e;
+    uint32_t status = 0;
+    PHYLO_CHECK(last_status(d_status, st, &status));
+    if (status) {
+        fprintf(stderr, "error: compare kernel reported device status %u\n", status);
+        return (int)cudaErrorLaunchTimeout;
+    }
+    return (int)cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // batched construction (new)
 // ---------------------------------------------------------------------------

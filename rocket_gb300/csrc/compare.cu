@@ -22,6 +22,8 @@
 // consumer indexes from the offset.
 #include "compare.cuh"
 
+#include <mutex>
+
 namespace phylo {
 
 constexpr int CMP_THREADS = 256;
@@ -314,6 +316,78 @@ cudaError_t compare_launch(cudaStream_t stream, void *scratch, size_t scratch_si
     k_intersect<<<grid, CMP_THREADS, kCmpSmem, stream>>>(lk, lv, nl, rk, rv, nr, splits, ntiles,
                                                         st, d_out);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Compare without caller-provided scratch.
+//
+// Some callers cannot call cudaMalloc at all: a host runtime that carved all of
+// the device memory into fixed cache slots when it started (as Rocket's device
+// cache does) and has nothing left to hand out for scratch, or a caller whose
+// device memory belongs to another framework's allocator and must not be taken
+// behind its back.  For them the pair kernels can also run on a scratch area
+// that is part of this library's image: one file-scope device array of fixed
+// size, loaded with the module on every GPU that uses the library and kept
+// there until the process exits.
+//
+// Limit: the two vectors may hold at most kStaticCompareMaxEntries entries
+// together (2^26 = 67,108,864), which needs kStaticCompareBytes of scratch.
+// All calls share the one array and it keeps what the last call left in it;
+// the partition kernel clears the completion ticket and the status word at the
+// start of every call, and every other byte a call reads it wrote first.  Two
+// calls whose kernels overlap on the GPU (different streams, or different host
+// threads) would race on the array, so such calls must be serialised.
+// ---------------------------------------------------------------------------
+
+constexpr uint64_t kStaticCompareMaxEntries = 1ull << 26;
+constexpr size_t kStaticCompareBytes =
+    (((kStaticCompareMaxEntries + CMP_TILE - 1) / CMP_TILE + 2) * sizeof(uint32_t) + 255) / 256 *
+        256 +
+    (sizeof(CmpState) + 255) / 256 * 256;
+
+static __device__ __align__(256) unsigned char g_static_compare_scratch[kStaticCompareBytes];
+
+uint64_t compare_static_max_entries() { return kStaticCompareMaxEntries; }
+size_t compare_static_bytes() { return kStaticCompareBytes; }
+
+// The host name of the array is only a stand-in; the device address comes from
+// cudaGetSymbolAddress, looked up once per device with that device current.
+static cudaError_t static_scratch_address(void **ptr) {
+    static std::mutex mu;
+    static void *addr[64] = {nullptr};
+    int dev = 0;
+    PHYLO_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_compare_scratch);
+        if (e != cudaSuccess) {
+            fprintf(stderr, "phylogenetics: cudaGetSymbolAddress of the static scratch failed: %s\n",
+                    cudaGetErrorString(e));
+            return e;
+        }
+        addr[dev] = p;
+    }
+    *ptr = addr[dev];
+    return cudaSuccess;
+}
+
+cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const float *lv,
+                                  uint32_t nl, const uint32_t *rk, const float *rv, uint32_t nr,
+                                  double *d_out, uint32_t **status_out) {
+    if ((uint64_t)nl + nr > kStaticCompareMaxEntries) {
+        fprintf(stderr,
+                "error: vectors of %u and %u entries exceed the %llu entries the built-in scratch "
+                "of compareCompositionVectorsStatic holds; use compareCompositionVectors with "
+                "caller scratch\n",
+                nl, nr, (unsigned long long)kStaticCompareMaxEntries);
+        return cudaErrorInvalidValue;
+    }
+    void *scratch = nullptr;
+    PHYLO_CHECK(static_scratch_address(&scratch));
+    return compare_launch(stream, scratch, kStaticCompareBytes, lk, lv, nl, rk, rv, nr, d_out,
+                          status_out);
 }
 
 }  // namespace phylo

@@ -13,4 +13,13 @@ cudaError_t compare_launch(cudaStream_t stream, void *scratch, size_t scratch_si
                            const uint32_t *lk, const float *lv, uint32_t nl, const uint32_t *rk,
                            const float *rv, uint32_t nr, double *d_out, uint32_t **status_out);
 
+// Same kernels on the library's built-in scratch array (no caller scratch, no
+// allocation); at most compare_static_max_entries() entries in the two vectors.
+// The first call on a device looks the array's address up (cudaGetSymbolAddress).
+cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const float *lv,
+                                  uint32_t nl, const uint32_t *rk, const float *rv, uint32_t nr,
+                                  double *d_out, uint32_t **status_out);
+uint64_t compare_static_max_entries();
+size_t compare_static_bytes();
+
 }  // namespace phylo
