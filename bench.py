@@ -168,6 +168,80 @@ def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed
     }
 
 
+def plain_path(arena, wl, seq, dev, n_pairs, n_build, peak, sample_pairs=400, sample_builds=16,
+               seed=7):
+    """The drop-in path as the reference drives it: one synchronous
+    buildCompositionVector per proteome and one synchronous
+    compareCompositionVectors per pair (CompositionVectorKernels.java:91-135),
+    timed on a sample and extrapolated.  Also the merge-path kernel alone:
+    asynchronous back-to-back pairs (random pairs, so the two vectors are not
+    L2-resident), algorithmic bytes 8*(nl+nr) per pair over the event time."""
+    import torch
+    from rocket_gb300 import _native
+    from rocket_gb300.kernels import CompositionVectorKernels
+    L = _native.load()
+    rng = np.random.default_rng(seed)
+    maxn = int(arena.nnz.max())
+    ker = CompositionVectorKernels("protein", 6, maxn + 1024, int(wl.lengths().max()), device=dev)
+    st = ker.stream
+    keys = torch.empty(maxn + 1024, dtype=torch.int32, device=dev)
+    vals = torch.empty(maxn + 1024, dtype=torch.float32, device=dev)
+    ids = rng.choice(len(wl), min(sample_builds, len(wl)), replace=False)
+    for i in ids[:2]:  # warm-up
+        ker.build_vector_gpu(seq[int(wl.offsets[i]):int(wl.offsets[i + 1])], keys, vals)
+    t0 = time.perf_counter()
+    for i in ids:
+        ker.build_vector_gpu(seq[int(wl.offsets[i]):int(wl.offsets[i + 1])], keys, vals)
+    t_build = (time.perf_counter() - t0) / len(ids)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    pi = rng.integers(0, arena.n, size=sample_pairs)
+    pj = (pi + 1 + rng.integers(0, arena.n - 1, size=sample_pairs)) % arena.n
+
+    def vec(v):
+        o, m = int(arena.off[v]), int(arena.nnz[v])
+        return arena.keys[o:o + m], arena.values[o:o + m], m
+
+    for a, b in zip(pi[:4], pj[:4]):  # warm-up
+        ka, va, na = vec(a)
+        kb, vb, nb = vec(b)
+        ker.compare_vectors_gpu(ka, va, na, kb, vb, nb, out)
+    t0 = time.perf_counter()
+    for a, b in zip(pi, pj):
+        ka, va, na = vec(a)
+        kb, vb, nb = vec(b)
+        ker.compare_vectors_gpu(ka, va, na, kb, vb, nb, out)
+    t_pair = (time.perf_counter() - t0) / sample_pairs
+    # kernel alone, asynchronous
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    nbytes = 0
+    torch.cuda.synchronize()
+    e0.record(st)
+    for a, b in zip(pi, pj):
+        ka, va, na = vec(a)
+        kb, vb, nb = vec(b)
+        _native.check(L.phyloComparePairAsync(
+            st.cuda_stream, ker.scratch.data_ptr(), ker.scratch.numel(), ka.data_ptr(),
+            va.data_ptr(), na, kb.data_ptr(), vb.data_ptr(), nb, out.data_ptr()))
+        nbytes += 8 * (na + nb)
+    e1.record(st)
+    torch.cuda.synchronize()
+    k_s = e0.elapsed_time(e1) / 1000.0
+    gbs = nbytes / k_s / 1e9
+    total = n_build * t_build + n_pairs * t_pair
+    return {
+        "value": n_pairs / total, "unit": "pairs/s",
+        "sample": (f"{len(ids)} synchronous buildCompositionVector calls ({1000 * t_build:.2f} ms "
+                   f"each) + {sample_pairs} synchronous compareCompositionVectors calls "
+                   f"({1000 * t_pair:.3f} ms each), extrapolated to {n_build} builds + "
+                   f"{n_pairs} pairs"),
+        "merge_kernel": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "pairs_per_s": sample_pairs / k_s,
+                         "note": "phyloComparePairAsync back to back on random pairs; algorithmic "
+                                 "bytes 8*(nl+nr); includes the partition kernel"},
+    }
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -345,6 +419,8 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "gpu_launches": int(launches),
     }
+    if not args.no_plain:
+        line["plain"] = plain_path(arena, wl, seq, dev, n_pairs, N, peak)
     if not args.no_cpu_baseline:
         cb = cpu_baseline(wl, n_pairs, N, seconds=args.ref_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -353,6 +429,88 @@ def run_ours(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+# ----------------------------------------------------------------------------
+# serving
+# ----------------------------------------------------------------------------
+
+SERVE_TEXT = ("serve2048: device-resident database of 2,048 synthetic proteomes (seed 4, protein "
+              "counts lognormal median 1,900 sigma 0.9 clipped to [300, 12,000]), K=6; query "
+              "batches of U(1..64) proteomes of the same distribution arriving as a Poisson "
+              "process; each query built, compared with the whole database, then appended; "
+              "HBM budget 120 GB")
+
+
+def run_serve(args):
+    import torch
+    from rocket_gb300 import synth
+    from rocket_gb300.engine import EngineConfig
+    from rocket_gb300.serve import Request, ServingEngine, percentile
+
+    rng = np.random.default_rng(4)
+    sizes = rng.integers(1, 65, size=args.query_batches)
+    n_db = args.db
+    total_q = int(sizes.sum())
+    t0 = time.perf_counter()
+    wl = synth.workload("serve2048", n=n_db, extra=total_q + args.warmup)
+    t_gen = time.perf_counter() - t0
+    db = wl.subset(range(n_db))
+    srv = ServingEngine("protein", 6, budget_bytes=args.budget_gb * 1e9, slots=args.slots,
+                        max_batch=64, cfg=EngineConfig(wshift=args.wshift, fold=args.fold,
+                                                       segments=args.segments))
+    lens = db.lengths()
+    capacity_entries = int(min(np.sum(8 * wl.lengths() + 64),
+                               (args.budget_gb * 1e9 - 20e9) / 8.0))
+    t0 = time.perf_counter()
+    srv.load(db, capacity_vectors=len(wl), capacity_entries=capacity_entries)
+    torch.cuda.synchronize()
+    t_load = time.perf_counter() - t0
+    srv.start()
+    nxt = n_db
+    # warm-up requests (one proteome each), not measured
+    for w in range(args.warmup):
+        r = srv.submit(Request(-1 - w, wl.subset([nxt]), append=False))
+        nxt += 1
+        r.done.wait(600)
+    batches = []
+    for b in range(args.query_batches):
+        batches.append(wl.subset(range(nxt, nxt + int(sizes[b]))))
+        nxt += int(sizes[b])
+    gaps = rng.exponential(1.0 / args.rate, size=args.query_batches)
+    reqs = []
+    t_start = time.perf_counter()
+    t_next = t_start
+    with ClockSampler(0) as clocks:
+        for b, q in enumerate(batches):
+            t_next += gaps[b]
+            delay = t_next - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            reqs.append(srv.submit(Request(b, q, append=True, t_arrival=time.perf_counter())))
+        for r in reqs:
+            r.done.wait(3600)
+        srv.stop()
+    errors = [r.error for r in reqs if r.error]
+    lat = [1000.0 * r.latency for r in reqs if not r.error]
+    t_end = max(r.t_done for r in reqs)
+    pairs = sum(len(r.proteomes) * r.db_n for r in reqs if not r.error)
+    line = {
+        "metric": "serve latency per query batch", "p50_ms": percentile(lat, 50),
+        "p99_ms": percentile(lat, 99), "max_ms": max(lat) if lat else None,
+        "value": pairs / (t_end - t_start), "unit": "pairs/s (sustained)",
+        "requests": len(reqs), "query_proteomes": total_q, "errors": len(errors),
+        "arrival_rate_per_s": args.rate, "slots": args.slots, "batches_run": srv.batches,
+        "db_start": n_db, "db_end": srv.db.arena.n, "db_appends_refused": srv.db.refused,
+        "hbm_budget_gb": args.budget_gb, "hbm_reserved_peak_gb": srv.budget.peak / 1e9,
+        "db_load_s": t_load, "generate_s": t_gen, "data": "synthetic",
+        "config": {"workload": SERVE_TEXT, "segments": args.segments, "window_shift": args.wshift},
+        "clocks": clocks.summary(),
+    }
+    if errors:
+        line["first_error"] = errors[0]
+    print(json.dumps(line), flush=True)
+    return 0 if not errors else 1
 
 
 def main():
@@ -367,9 +525,19 @@ def main():
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the per-pair ABI measurement")
     ap.add_argument("--proteomes", type=int, default=None,
                     help="use only the first N proteomes (small profiling cases)")
+    ap.add_argument("--mode", default="allpairs", choices=["allpairs", "serve"])
+    ap.add_argument("--db", type=int, default=2048, help="serve: database proteomes")
+    ap.add_argument("--query-batches", type=int, default=24, help="serve: arriving query batches")
+    ap.add_argument("--rate", type=float, default=8.0, help="serve: query batches per second")
+    ap.add_argument("--slots", type=int, default=2, help="serve: concurrent batches")
+    ap.add_argument("--segments", type=int, default=16, help="serve: key segments per tile")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: HBM budget")
     args = ap.parse_args()
+    if args.mode == "serve":
+        return run_serve(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -141,9 +141,11 @@ int phyloBuildLaunchesPerBatch(void);
  * ------------------------------------------------------------------------- */
 
 /* Window index of an arena: d_roff uint32[num_vectors][num_windows + 1],
- * entry [v][r] = number of entries of vector v with key < r << window_shift. */
+ * entry [v][r] = number of entries of vector v with key < r << window_shift.
+ * max_vector_len bounds the (padded) length of every vector. */
 int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors,
-                     int window_shift, unsigned int num_windows, uintptr_t d_roff);
+                     int window_shift, unsigned int num_windows, long max_vector_len,
+                     uintptr_t d_roff);
 
 /* Sets the pair kernel's shared-memory limit for this window width (4..11)
  * and reports how many CTAs fit on one SM. */
@@ -153,14 +155,17 @@ int phyloPairsPrepare(int window_shift, int *ctas_per_sm);
 int phyloPairsSmemBytes(int window_shift);
 
 /* Pair kernel over num_items work items (8 uint32 each: row0, nrow, col0,
- * ncol, w0, w1, part, tile); d_counter (uint32) must be 0; partial blocks of
- * 16 x 256 float pairs go to d_part; d_item_cycles (int64[num_items]) may be 0.
- * Asynchronous. */
-int phyloPairsLaunch(uintptr_t stream, uintptr_t d_keys, uintptr_t d_values, uintptr_t d_vec_off,
-                     uintptr_t d_roff, unsigned int num_windows, int window_shift,
-                     uintptr_t d_rowids, uintptr_t d_colids, uintptr_t d_items, int num_items,
-                     uintptr_t d_counter, uintptr_t d_part, int fold, uintptr_t d_item_cycles,
-                     int grid);
+ * ncol, w0, w1, part, tile).  Row vectors are read from the row arena and
+ * column vectors from the column arena (pass the same arena twice for the
+ * pairs of one set; a query batch against a resident database passes two).
+ * d_counter (uint32) must be 0; partial blocks of 16 x 256 float pairs go to
+ * d_part; d_item_cycles (int64[num_items]) may be 0.  Asynchronous. */
+int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_values,
+                     uintptr_t d_row_vec_off, uintptr_t d_row_roff, uintptr_t d_col_keys,
+                     uintptr_t d_col_values, uintptr_t d_col_vec_off, uintptr_t d_col_roff,
+                     unsigned int num_windows, int window_shift, uintptr_t d_rowids,
+                     uintptr_t d_colids, uintptr_t d_items, int num_items, uintptr_t d_counter,
+                     uintptr_t d_part, int fold, uintptr_t d_item_cycles, int grid);
 
 /* Sums the partial blocks of each tile (4 uint32: row0, nrow, col0, ncol) into
  * d_out[rowid * ldc + colid] (double); `upper` keeps pairs whose row position
@@ -170,9 +175,13 @@ int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int 
                      long ldc, int upper, int mirror);
 
 /* d_out[v * ldc + v] = sum of squares of vector v (the diagonal the
- * reference's run includes, phylogenetics_analysis/Main.java:196). */
+ * reference's run includes, phylogenetics_analysis/Main.java:196); d_part is
+ * device scratch of phyloSelfDotPartBytes bytes. */
 int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int num_vectors,
-                 uintptr_t d_out, long ldc);
+                 long max_vector_len, uintptr_t d_part, uintptr_t d_out, long ldc);
+
+/* Scratch bytes phyloSelfDot needs. */
+long phyloSelfDotPartBytes(int num_vectors, long max_vector_len);
 
 /* compareCompositionVectors without the synchronisation (result left on the
  * device); scratch from estimateScratchMemory. */

@@ -80,20 +80,23 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloBuildLaunchesPerBatch.argtypes = []
     L.phyloBuildLaunchesPerBatch.restype = c_int
     # pair engine
-    L.phyloWindowIndex.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_int, c_uint, c_ptr]
+    L.phyloWindowIndex.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_int, c_uint, c_long, c_ptr]
     L.phyloWindowIndex.restype = c_int
     L.phyloPairsPrepare.argtypes = [c_int, ctypes.POINTER(c_int)]
     L.phyloPairsPrepare.restype = c_int
     L.phyloPairsSmemBytes.argtypes = [c_int]
     L.phyloPairsSmemBytes.restype = c_int
-    L.phyloPairsLaunch.argtypes = [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_uint, c_int, c_ptr, c_ptr,
-                                   c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int]
+    L.phyloPairsLaunch.argtypes = [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                                   c_uint, c_int, c_ptr, c_ptr, c_ptr, c_int, c_ptr, c_ptr, c_int,
+                                   c_ptr, c_int]
     L.phyloPairsLaunch.restype = c_int
     L.phyloPairsReduce.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_int, c_ptr, c_ptr, c_ptr, c_long,
                                    c_int, c_int]
     L.phyloPairsReduce.restype = c_int
-    L.phyloSelfDot.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_ptr, c_long]
+    L.phyloSelfDot.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_long, c_ptr, c_ptr, c_long]
     L.phyloSelfDot.restype = c_int
+    L.phyloSelfDotPartBytes.argtypes = [c_int, c_long]
+    L.phyloSelfDotPartBytes.restype = c_long
     L.phyloComparePairAsync.argtypes = [c_ptr, c_ptr, c_long, c_ptr, c_ptr, c_int, c_ptr, c_ptr,
                                         c_int, c_ptr]
     L.phyloComparePairAsync.restype = c_int
@@ -105,7 +108,7 @@ EXPORTED = [
     "compareCompositionVectorsStatic", "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchEmit", "phyloBuildBatchNorms",
     "phyloBuildBatchCounts", "phyloBuildLaunchesPerBatch", "phyloWindowIndex",
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsLaunch", "phyloPairsReduce",
-    "phyloSelfDot", "phyloComparePairAsync",
+    "phyloSelfDot", "phyloSelfDotPartBytes", "phyloComparePairAsync",
 ]
 
 

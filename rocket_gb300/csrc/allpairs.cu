@@ -32,7 +32,10 @@
 
 namespace phylo {
 
-size_t ap_smem_bytes(uint32_t wshift) { return (((size_t)1 << wshift) + 1) * AP_TI * sizeof(float); }
+size_t ap_ring_bytes();
+size_t ap_smem_bytes(uint32_t wshift) {
+    return (((size_t)1 << wshift) + 1) * AP_TI * sizeof(float) + ap_ring_bytes();
+}
 
 int ap_max_wshift() { return 11; }
 
@@ -75,11 +78,44 @@ __device__ __forceinline__ void fold16(float (&acc)[16], float (&hi)[16], float 
     }
 }
 
+// Per-thread ring of 16-byte column groups (4 keys + 4 values) fetched with
+// cp.async, RING groups ahead of the one being used, so a thread's column stream
+// stays in flight across window barriers.
+constexpr int RING = 4;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_ring() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(RING - 1) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+size_t ap_ring_bytes() { return (size_t)RING * AP_THREADS * 32; }
+
+__device__ __forceinline__ FF ff_shfl_xor(FF v, int m) {
+    FF r;
+    r.hi = __shfl_xor_sync(0xffffffffu, v.hi, m);
+    r.lo = __shfl_xor_sync(0xffffffffu, v.lo, m);
+    return r;
+}
+
+// Column side: four lanes per column vector.  Lane q of a column streams the
+// column's 4-entry groups q, q+4, q+8, ... through its cp.async ring, so the four
+// lanes of a column fetch 64 contiguous bytes per load, and keeps its own 16
+// accumulators for the whole item; the four lanes' sums are combined once, at
+// the end of the item.
 __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
-    extern __shared__ __align__(16) float D[];  // (W + 1) x 16 floats
-    __shared__ uint32_t s_item;
+    extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t W = 1u << a.wshift, wmask = W - 1u;
+    float *D = reinterpret_cast<float *>(smem);                    // (W + 1) x 16
+    uint4 *ring_k = reinterpret_cast<uint4 *>(smem + (size_t)(W + 1) * 64);
+    float4 *ring_v = reinterpret_cast<float4 *>(ring_k + RING * AP_THREADS);
+    __shared__ uint32_t s_item;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t jcol = threadIdx.x / AP_LPC, q = threadIdx.x % AP_LPC;
     const uint32_t Rs = a.R + 1;
 
     for (uint32_t i = threadIdx.x; i < (W + 1) * 4u; i += AP_THREADS)
@@ -94,12 +130,30 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
         const ApItem item = a.items[it];
         const int64_t t_start = clock64();
 
-        // this thread's column
-        const bool has_col = threadIdx.x < item.ncol;
-        const uint32_t cv = has_col ? a.colids[item.col0 + threadIdx.x] : 0u;
-        const uint64_t cbase = a.vec_off[cv];
-        const uint32_t *cro = a.roff + (uint64_t)cv * Rs;
-        // this warp's rows: 2*warp, 2*warp + 1
+        // ---- column side
+        const bool has_col = jcol < item.ncol;
+        const uint32_t cv = has_col ? a.colids[item.col0 + jcol] : 0u;
+        const uint64_t cbase = a.col.vec_off[cv];
+        const uint32_t *cro = a.col.roff + (uint64_t)cv * Rs;
+        uint32_t c_lo = has_col ? __ldg(&cro[item.w0]) : 0u;
+        const uint32_t c_end = has_col ? __ldg(&cro[item.w1]) : 0u;
+        uint32_t c_hi_next = has_col ? __ldg(&cro[item.w0 + 1]) : 0u;
+        // this lane's groups start at entry (c_lo & ~3) + 4q and advance by 16
+        uint32_t cur = (c_lo & ~3u) + 4 * q;  // first entry of the oldest unreleased group
+        uint32_t fetch = cur;                  // next group to fetch
+        uint32_t slot_cur = 0, slot_fetch = 0;
+#pragma unroll
+        for (int k = 0; k < RING; k++) {
+            if (fetch < c_end) {
+                cp_async16(&ring_k[slot_fetch * AP_THREADS + threadIdx.x], a.col.keys + cbase + fetch);
+                cp_async16(&ring_v[slot_fetch * AP_THREADS + threadIdx.x], a.col.vals + cbase + fetch);
+            }
+            fetch += 4 * AP_LPC;
+            slot_fetch = (slot_fetch + 1) & (RING - 1);
+            cp_async_commit();
+        }
+
+        // ---- this warp's rows (2*warp, 2*warp + 1)
         uint32_t rv[2];
         uint64_t rbase[2];
         bool has_row[2];
@@ -108,61 +162,95 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
             const uint32_t row = 2 * warp + k;
             has_row[k] = row < item.nrow;
             rv[k] = has_row[k] ? a.rowids[item.row0 + row] : 0u;
-            rbase[k] = a.vec_off[rv[k]];
+            rbase[k] = a.row.vec_off[rv[k]];
         }
-
         float acc[16], hi[16], lo[16];
 #pragma unroll
         for (int i = 0; i < 16; i++) acc[i] = hi[i] = lo[i] = 0.0f;
         uint32_t nacc = 0;
 
-        // window offsets: rows via lane-held prefetch of 32 windows, column
-        // one window ahead
+        // row window offsets: lane-held for 32 windows; first 32 entries of each
+        // row's next window prefetched into registers
         uint32_t r_lo[2] = {0, 0}, r_hi[2] = {0, 0};
         uint32_t wb = item.w0;
-        uint32_t c_lo = has_col ? __ldg(&cro[item.w0]) : 0u;
-        uint32_t c_hi_next = has_col ? __ldg(&cro[item.w0 + 1]) : 0u;
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            if (has_row[k]) {
+                const uint32_t *ro = a.row.roff + (uint64_t)rv[k] * Rs;
+                r_lo[k] = __ldg(&ro[min(item.w0 + lane, a.R)]);
+                r_hi[k] = __ldg(&ro[min(item.w0 + lane + 1, a.R)]);
+            }
+        }
+        uint32_t pk[2] = {0xffffffffu, 0xffffffffu};
+        float pv[2] = {0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const uint32_t lo_k = __shfl_sync(0xffffffffu, r_lo[k], 0);
+            const uint32_t hi_k = __shfl_sync(0xffffffffu, r_hi[k], 0);
+            if (has_row[k] && lo_k + lane < hi_k) {
+                pk[k] = __ldg(&a.row.keys[rbase[k] + lo_k + lane]);
+                pv[k] = __ldg(&a.row.vals[rbase[k] + lo_k + lane]);
+            }
+        }
 
         for (uint32_t r = item.w0; r < item.w1; r++) {
-            if (r == item.w0 || r - wb >= 32u) {
-                wb = r;
-#pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    if (has_row[k]) {
-                        const uint32_t *ro = a.roff + (uint64_t)rv[k] * Rs;
-                        r_lo[k] = __ldg(&ro[min(r + lane, a.R)]);
-                        r_hi[k] = __ldg(&ro[min(r + lane + 1, a.R)]);
-                    }
-                }
-            }
             const int sl = (int)(r - wb);
-            const uint32_t c_hi = c_hi_next;
-            if (has_col && r + 2 <= a.R) c_hi_next = __ldg(&cro[r + 2]);
-            // densify this warp's rows
+            // densify window r: first 32 entries from registers, the rest loaded
+            uint32_t ck[2];
+            uint32_t lo_k[2], hi_k[2];
 #pragma unroll
             for (int k = 0; k < 2; k++) {
-                const uint32_t lo_k = __shfl_sync(0xffffffffu, r_lo[k], sl);
-                const uint32_t hi_k = __shfl_sync(0xffffffffu, r_hi[k], sl);
+                lo_k[k] = __shfl_sync(0xffffffffu, r_lo[k], sl);
+                hi_k[k] = __shfl_sync(0xffffffffu, r_hi[k], sl);
+                ck[k] = pk[k];
                 if (has_row[k]) {
                     const uint32_t row = 2 * warp + k;
-                    for (uint32_t e = lo_k + lane; e < hi_k; e += 32) {
-                        const uint32_t key = __ldg(&a.keys[rbase[k] + e]);
-                        D[d_slot(key & wmask, row)] = __ldg(&a.vals[rbase[k] + e]);
+                    if (pk[k] != 0xffffffffu) D[d_slot(pk[k] & wmask, row)] = pv[k];
+                    for (uint32_t e = lo_k[k] + 32 + lane; e < hi_k[k]; e += 32) {
+                        const uint32_t key = __ldg(&a.row.keys[rbase[k] + e]);
+                        D[d_slot(key & wmask, row)] = __ldg(&a.row.vals[rbase[k] + e]);
                     }
                 }
             }
+            // prefetch the next window's row offsets / first entries
+            if (r + 1 < item.w1) {
+                if (r + 1 - wb >= 32u) {
+                    wb = r + 1;
+#pragma unroll
+                    for (int k = 0; k < 2; k++) {
+                        if (has_row[k]) {
+                            const uint32_t *ro = a.row.roff + (uint64_t)rv[k] * Rs;
+                            r_lo[k] = __ldg(&ro[min(wb + lane, a.R)]);
+                            r_hi[k] = __ldg(&ro[min(wb + lane + 1, a.R)]);
+                        }
+                    }
+                }
+                const int sn = (int)(r + 1 - wb);
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const uint32_t nlo = __shfl_sync(0xffffffffu, r_lo[k], sn);
+                    const uint32_t nhi = __shfl_sync(0xffffffffu, r_hi[k], sn);
+                    pk[k] = 0xffffffffu;
+                    if (has_row[k] && nlo + lane < nhi) {
+                        pk[k] = __ldg(&a.row.keys[rbase[k] + nlo + lane]);
+                        pv[k] = __ldg(&a.row.vals[rbase[k] + nlo + lane]);
+                    }
+                }
+            }
+            const uint32_t c_hi = c_hi_next;
+            if (has_col && r + 2 <= a.R) c_hi_next = __ldg(&cro[r + 2]);
             __syncthreads();
-            // stream this thread's column entries [c_lo, c_hi)
-            if (has_col && c_hi > c_lo) {
-                const uint32_t g0 = c_lo & ~3u;
-                for (uint32_t g = g0; g < c_hi; g += 4) {
-                    const uint4 kk = __ldg(reinterpret_cast<const uint4 *>(a.keys + cbase + g));
-                    const float4 vv = __ldg(reinterpret_cast<const float4 *>(a.vals + cbase + g));
+            // this lane's groups of the column that start before c_hi
+            if (has_col) {
+                while (cur < c_hi) {
+                    cp_async_wait_ring();
+                    const uint4 kk = ring_k[slot_cur * AP_THREADS + threadIdx.x];
+                    const float4 vv = ring_v[slot_cur * AP_THREADS + threadIdx.x];
                     const uint32_t ks[4] = {kk.x, kk.y, kk.z, kk.w};
                     const float vs[4] = {vv.x, vv.y, vv.z, vv.w};
 #pragma unroll
                     for (int u = 0; u < 4; u++) {
-                        const uint32_t e = g + u;
+                        const uint32_t e = cur + u;
                         const bool ok = e >= c_lo && e < c_hi;
                         fma_entry(D, ok ? (ks[u] & wmask) : W, ok ? vs[u] : 0.0f, acc);
                     }
@@ -171,29 +259,46 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
                         fold16(acc, hi, lo);
                         nacc = 0;
                     }
+                    if (cur + 4 > c_hi) break;  // reaches into the next window: keep it
+                    if (fetch < c_end) {
+                        cp_async16(&ring_k[slot_fetch * AP_THREADS + threadIdx.x],
+                                   a.col.keys + cbase + fetch);
+                        cp_async16(&ring_v[slot_fetch * AP_THREADS + threadIdx.x],
+                                   a.col.vals + cbase + fetch);
+                    }
+                    fetch += 4 * AP_LPC;
+                    slot_fetch = (slot_fetch + 1) & (RING - 1);
+                    cp_async_commit();
+                    cur += 4 * AP_LPC;
+                    slot_cur = (slot_cur + 1) & (RING - 1);
                 }
             }
             c_lo = c_hi;
             __syncthreads();
-            // clear this warp's rows
+            // clear window r
 #pragma unroll
             for (int k = 0; k < 2; k++) {
-                const uint32_t lo_k = __shfl_sync(0xffffffffu, r_lo[k], sl);
-                const uint32_t hi_k = __shfl_sync(0xffffffffu, r_hi[k], sl);
                 if (has_row[k]) {
                     const uint32_t row = 2 * warp + k;
-                    for (uint32_t e = lo_k + lane; e < hi_k; e += 32) {
-                        const uint32_t key = __ldg(&a.keys[rbase[k] + e]);
+                    if (ck[k] != 0xffffffffu) D[d_slot(ck[k] & wmask, row)] = 0.0f;
+                    for (uint32_t e = lo_k[k] + 32 + lane; e < hi_k[k]; e += 32) {
+                        const uint32_t key = __ldg(&a.row.keys[rbase[k] + e]);
                         D[d_slot(key & wmask, row)] = 0.0f;
                     }
                 }
             }
         }
+        cp_async_wait_all();
         fold16(acc, hi, lo);
-        // partial block [16][256]
+        // combine the column's four lanes (fixed order), lane q writes rows q, q+4, ...
         FF *dst = a.part + (uint64_t)item.part * (AP_TI * AP_TJ);
 #pragma unroll
-        for (int i = 0; i < 16; i++) dst[i * AP_TJ + threadIdx.x] = FF{hi[i], lo[i]};
+        for (int i = 0; i < 16; i++) {
+            FF v = {hi[i], lo[i]};
+            v = ff_merge(v, ff_shfl_xor(v, 1));
+            v = ff_merge(v, ff_shfl_xor(v, 2));
+            if ((uint32_t)(i & 3) == q) dst[i * AP_TJ + jcol] = v;
+        }
         if (a.item_cycles && threadIdx.x == 0) a.item_cycles[it] = clock64() - t_start;
     }
 }
@@ -219,34 +324,46 @@ cudaError_t ap_launch(const ApArgs &a, int grid, cudaStream_t st) {
 // window index
 // ---------------------------------------------------------------------------
 
-// one CTA per vector
+constexpr uint32_t RI_SLICE = 16384;  // entries per CTA
+
+// grid = (slices, N): CTA (s, v) handles entries [s*RI_SLICE, (s+1)*RI_SLICE) of
+// vector v.  Window r gets the index of the first entry whose key is >= r << wshift;
+// the CTA holding the last real entry fills the windows after it.
 __global__ void k_range_index(const uint32_t *__restrict__ keys, const uint64_t *__restrict__ vec_off,
                               uint32_t R, uint32_t wshift, uint32_t *roff) {
-    const uint32_t v = blockIdx.x;
+    const uint32_t v = blockIdx.y;
     const uint64_t b = vec_off[v];
-    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);  // padded length may exceed nnz
+    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);  // padded length
     uint32_t *ro = roff + (uint64_t)v * (R + 1);
-    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const uint32_t e0 = blockIdx.x * RI_SLICE;
+    if (e0 >= n) {
+        if (n == 0 && blockIdx.x == 0)
+            for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
+        return;
+    }
+    const uint32_t e1 = min(n, e0 + RI_SLICE);
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const uint32_t key = keys[b + e];
         if (key == 0xffffffffu) continue;  // padding
         const uint32_t rt = min(key >> wshift, R);
-        const uint32_t prev = e == 0 ? 0u : keys[b + e - 1];
-        const int64_t rp = (e == 0) ? -1 : (int64_t)min(prev >> wshift, R);
+        const int64_t rp = e == 0 ? -1 : (int64_t)min(keys[b + e - 1] >> wshift, R);
         for (int64_t r = rp + 1; r <= (int64_t)rt; r++) ro[r] = e;
+        // last real entry: the next key is padding or the end
+        const bool last = (e + 1 == n) || keys[b + e + 1] == 0xffffffffu;
+        if (last)
+            for (uint32_t r = rt + 1; r <= R; r++) ro[r] = e + 1;
     }
-    // tail: windows after the last real key get the real length
-    if (threadIdx.x == 0) {
-        uint32_t m = n;
-        while (m > 0 && keys[b + m - 1] == 0xffffffffu) m--;
-        const int64_t rl = m == 0 ? -1 : (int64_t)min(keys[b + m - 1] >> wshift, R);
-        for (int64_t r = rl + 1; r <= (int64_t)R; r++) ro[r] = m;
-    }
+    // a vector made only of padding
+    if (blockIdx.x == 0 && keys[b] == 0xffffffffu)
+        for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
 }
 
 cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
-                               uint32_t R, uint32_t wshift, uint32_t *roff, cudaStream_t st) {
+                               uint32_t R, uint32_t wshift, uint32_t *roff, cudaStream_t st,
+                               uint64_t max_len) {
     if (N == 0) return cudaSuccess;
-    k_range_index<<<N, 256, 0, st>>>(keys, vec_off, R, wshift, roff);
+    const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, RI_SLICE);
+    k_range_index<<<dim3(slices, N), 256, 0, st>>>(keys, vec_off, R, wshift, roff);
     return cudaGetLastError();
 }
 
@@ -287,12 +404,16 @@ cudaError_t ap_reduce_launch(const ApReduceArgs &r, cudaStream_t st) {
 // self products (the diagonal of the reference's run, Main.java:196)
 // ---------------------------------------------------------------------------
 
+constexpr uint32_t SD_SLICE = 65536;  // entries per CTA
+
+// grid = (slices, N): float-float sum of squares of one slice -> part[v * slices + s]
 __global__ void k_self_dot(const float *__restrict__ vals, const uint64_t *__restrict__ vec_off,
-                           double *out, uint64_t ldc) {
-    const uint32_t v = blockIdx.x;
+                           uint32_t slices, FF *part) {
+    const uint32_t v = blockIdx.y;
     const uint64_t b = vec_off[v], n = vec_off[v + 1] - b;
+    const uint64_t e0 = (uint64_t)blockIdx.x * SD_SLICE, e1 = min(n, e0 + SD_SLICE);
     FF acc = {0.0f, 0.0f};
-    for (uint64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const float x = vals[b + e];
         float p, q;
         two_prod(x, x, p, q);
@@ -304,20 +425,37 @@ __global__ void k_self_dot(const float *__restrict__ vals, const uint64_t *__res
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
-        DD d = {0.0, 0.0};
-        for (int w = 0; w < (int)(blockDim.x / 32); w++) {
-            dd_add(d, (double)ws[w].hi);
-            dd_add(d, (double)ws[w].lo);
-        }
-        out[(uint64_t)v * ldc + v] = __dadd_rn(d.hi, d.lo);
+        FF t = {0.0f, 0.0f};
+        for (int w = 0; w < (int)(blockDim.x / 32); w++) t = ff_merge(t, ws[w]);
+        part[(uint64_t)v * slices + blockIdx.x] = t;
     }
 }
 
+__global__ void k_self_dot_final(const FF *part, uint32_t slices, uint32_t N, double *out,
+                                 uint64_t ldc) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= N) return;
+    DD d = {0.0, 0.0};
+    for (uint32_t s = 0; s < slices; s++) {
+        const FF f = part[(uint64_t)v * slices + s];
+        dd_add(d, (double)f.hi);
+        dd_add(d, (double)f.lo);
+    }
+    out[(uint64_t)v * ldc + v] = __dadd_rn(d.hi, d.lo);
+}
+
+// part must hold N * slices float pairs, slices = ceil(max_len / SD_SLICE)
 cudaError_t self_dot_launch(const float *vals, const uint64_t *vec_off, uint32_t N, double *out,
-                            uint64_t ldc, cudaStream_t st) {
+                            uint64_t ldc, uint64_t max_len, FF *part, cudaStream_t st) {
     if (N == 0) return cudaSuccess;
-    k_self_dot<<<N, 256, 0, st>>>(vals, vec_off, out, ldc);
+    const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, SD_SLICE);
+    k_self_dot<<<dim3(slices, N), 256, 0, st>>>(vals, vec_off, slices, part);
+    k_self_dot_final<<<(N + 127) / 128, 128, 0, st>>>(part, slices, N, out, ldc);
     return cudaGetLastError();
+}
+
+uint64_t self_dot_part_count(uint32_t N, uint64_t max_len) {
+    return (uint64_t)N * div_up(max_len ? max_len : 1, SD_SLICE);
 }
 
 }  // namespace phylo

@@ -5,10 +5,11 @@
 namespace phylo {
 
 constexpr int AP_TI = 16;             // row vectors per item (densified in shared memory)
-constexpr int AP_THREADS = 256;       // one column vector per thread
-constexpr int AP_TJ = AP_THREADS;     // column vectors per item
+constexpr int AP_THREADS = 256;
+constexpr int AP_LPC = 4;             // lanes per column vector
+constexpr int AP_TJ = AP_THREADS / AP_LPC;  // column vectors per item
 
-// One unit of work: up to 16 row vectors x 256 column vectors over the key
+// One unit of work: up to 16 row vectors x 64 column vectors over the key
 // windows [w0, w1).  Vectors are named by positions in rowids / colids.
 struct ApItem {
     uint32_t row0, nrow;  // rows: rowids[row0 .. row0 + nrow)
@@ -18,11 +19,17 @@ struct ApItem {
     uint32_t tile;        // tile this item contributes to
 };
 
-struct ApArgs {
+// Rows and columns may live in different arenas (e.g. arriving queries against
+// a resident database); for all pairs of one arena both sides are the same.
+struct ApArena {
     const uint32_t *keys;
     const float *vals;
     const uint64_t *vec_off;   // [N+1] arena offsets, each a multiple of 4 entries
     const uint32_t *roff;      // [N][R+1] window index
+};
+
+struct ApArgs {
+    ApArena row, col;
     uint32_t R;                // windows per vector
     uint32_t wshift;           // window width = 1 << wshift keys
     const uint32_t *rowids, *colids;
@@ -41,7 +48,8 @@ cudaError_t ap_launch(const ApArgs &a, int grid, cudaStream_t st);
 
 // window index: roff[v][r] = number of entries of vector v with key < r << wshift
 cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
-                               uint32_t R, uint32_t wshift, uint32_t *roff, cudaStream_t st);
+                               uint32_t R, uint32_t wshift, uint32_t *roff, cudaStream_t st,
+                               uint64_t max_len);
 
 // Tile t (rows rowids[row0..], columns colids[col0..]) has S partial blocks
 // part[t * S + s].  Writes out[rowid * ldc + colid] (and the mirrored entry
@@ -61,7 +69,9 @@ struct ApReduceArgs {
 cudaError_t ap_reduce_launch(const ApReduceArgs &r, cudaStream_t st);
 
 // C of each vector with itself (sum of squares, float-float): out[v*ldc+v].
+// `part` holds self_dot_part_count(N, max_len) float pairs.
 cudaError_t self_dot_launch(const float *vals, const uint64_t *vec_off, uint32_t N, double *out,
-                            uint64_t ldc, cudaStream_t st);
+                            uint64_t ldc, uint64_t max_len, FF *part, cudaStream_t st);
+uint64_t self_dot_part_count(uint32_t N, uint64_t max_len);
 
 }  // namespace phylo

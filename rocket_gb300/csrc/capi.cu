@@ -359,10 +359,12 @@ int phyloBuildLaunchesPerBatch(void) { return build_launches_per_batch(); }
 
 // Window index of an arena: roff uint32[num_vectors][R + 1], R = ceil(key_limit / 2^shift).
 int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors,
-                     int window_shift, unsigned int num_windows, uintptr_t d_roff) {
+                     int window_shift, unsigned int num_windows, long max_vector_len,
+                     uintptr_t d_roff) {
     return (int)range_index_launch((const uint32_t *)d_keys, (const uint64_t *)d_vec_off,
                                    (uint32_t)num_vectors, num_windows, (uint32_t)window_shift,
-                                   (uint32_t *)d_roff, (cudaStream_t)stream);
+                                   (uint32_t *)d_roff, (cudaStream_t)stream,
+                                   (uint64_t)max_vector_len);
 }
 
 // Sets the kernel's shared-memory limit for this window width and reports the
@@ -374,18 +376,25 @@ int phyloPairsPrepare(int window_shift, int *ctas_per_sm) {
 
 int phyloPairsSmemBytes(int window_shift) { return (int)ap_smem_bytes((uint32_t)window_shift); }
 
-// Launches the pair kernel over `num_items` items (8 uint32 each, see ApItem).
-// d_counter must be zero.  d_item_cycles may be 0.
-int phyloPairsLaunch(uintptr_t stream, uintptr_t d_keys, uintptr_t d_values, uintptr_t d_vec_off,
-                     uintptr_t d_roff, unsigned int num_windows, int window_shift,
-                     uintptr_t d_rowids, uintptr_t d_colids, uintptr_t d_items, int num_items,
-                     uintptr_t d_counter, uintptr_t d_part, int fold, uintptr_t d_item_cycles,
-                     int grid) {
+// Launches the pair kernel over `num_items` items (8 uint32 each, see ApItem);
+// row vectors come from the row arena, column vectors from the column arena
+// (the same arena for all pairs of one set).  d_counter must be zero.
+// d_item_cycles may be 0.
+int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_values,
+                     uintptr_t d_row_vec_off, uintptr_t d_row_roff, uintptr_t d_col_keys,
+                     uintptr_t d_col_values, uintptr_t d_col_vec_off, uintptr_t d_col_roff,
+                     unsigned int num_windows, int window_shift, uintptr_t d_rowids,
+                     uintptr_t d_colids, uintptr_t d_items, int num_items, uintptr_t d_counter,
+                     uintptr_t d_part, int fold, uintptr_t d_item_cycles, int grid) {
     ApArgs a;
-    a.keys = (const uint32_t *)d_keys;
-    a.vals = (const float *)d_values;
-    a.vec_off = (const uint64_t *)d_vec_off;
-    a.roff = (const uint32_t *)d_roff;
+    a.row.keys = (const uint32_t *)d_row_keys;
+    a.row.vals = (const float *)d_row_values;
+    a.row.vec_off = (const uint64_t *)d_row_vec_off;
+    a.row.roff = (const uint32_t *)d_row_roff;
+    a.col.keys = (const uint32_t *)d_col_keys;
+    a.col.vals = (const float *)d_col_values;
+    a.col.vec_off = (const uint64_t *)d_col_vec_off;
+    a.col.roff = (const uint32_t *)d_col_roff;
     a.R = num_windows;
     a.wshift = (uint32_t)window_shift;
     a.rowids = (const uint32_t *)d_rowids;
@@ -418,10 +427,14 @@ int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int 
 }
 
 int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int num_vectors,
-                 uintptr_t d_out, long ldc) {
+                 long max_vector_len, uintptr_t d_part, uintptr_t d_out, long ldc) {
     return (int)self_dot_launch((const float *)d_values, (const uint64_t *)d_vec_off,
                                 (uint32_t)num_vectors, (double *)d_out, (uint64_t)ldc,
-                                (cudaStream_t)stream);
+                                (uint64_t)max_vector_len, (FF *)d_part, (cudaStream_t)stream);
+}
+
+long phyloSelfDotPartBytes(int num_vectors, long max_vector_len) {
+    return (long)(self_dot_part_count((uint32_t)num_vectors, (uint64_t)max_vector_len) * sizeof(FF));
 }
 
 // Pair kernel launch on raw arena pointers for one pair, through the merge

@@ -69,9 +69,138 @@ __device__ __forceinline__ float markov_alpha(uint32_t full, uint32_t prefix, ui
     return __double2float_rn(__ddiv_rn(__dsub_rn(p, p0), p0));
 }
 
+// The same alpha with the FP64 work cut down (GB300 issues FP64 at a small
+// fraction of the FP32 rate):
+//   * p, prefix/n1, suffix/n1, middle/n2 come from per-proteome tables holding
+//     exactly those IEEE quotients for counts below PROB_TABLE;
+//   * p0 = RN(a / b) as q0 = RN(a * y), r = a - b*q0 (exact by FMA),
+//     RN(q0 + r*y) with y = RN(1/b) from the table -- a correctly rounded
+//     quotient (Markstein's reciprocal-correction theorem);
+//   * (p - p0) / p0 is only needed rounded to float: a quotient accurate to
+//     ~2^-46 from a float reciprocal and one FMA correction gives the same float
+//     unless it lies within 256 double ulps of a float rounding midpoint, where
+//     the exact IEEE division is used instead.
+// Anything outside the tables (large counts, no K-windows) takes markov_alpha.
+__device__ __forceinline__ float markov_alpha_fast(uint32_t full, uint32_t prefix,
+                                                   uint32_t suffix, uint32_t middle, uint32_t n0,
+                                                   uint32_t n1, uint32_t n2,
+                                                   const double *__restrict__ prob) {
+    if (full == 0u && n0 != 0u) return -1.0f;
+    if (n0 == 0u || full >= PROB_TABLE || prefix >= PROB_TABLE || suffix >= PROB_TABLE ||
+        middle >= PROB_TABLE)
+        return markov_alpha(full, prefix, suffix, middle, n0, n1, n2);
+    const double p = __ldg(&prob[full]);
+    const double pp = __ldg(&prob[PROB_TABLE + prefix]);
+    const double ps = __ldg(&prob[PROB_TABLE + suffix]);
+    const double pm = __ldg(&prob[2 * PROB_TABLE + middle]);
+    const double ym = __ldg(&prob[3 * PROB_TABLE + middle]);
+    const double a = __dmul_rn(pp, ps);
+    const double q0 = __dmul_rn(a, ym);
+    const double p0 = __fma_rn(__fma_rn(-q0, pm, a), ym, q0);
+    const double d = __dsub_rn(p, p0);
+    if (d == 0.0) return 0.0f;
+    const double y0 = (double)__frcp_rn(__double2float_rn(p0));
+    const double g0 = __dmul_rn(d, y0);
+    const double g1 = __fma_rn(__fma_rn(-g0, p0, d), y0, g0);
+    const long long low = (long long)(__double_as_longlong(g1) & ((1ll << 29) - 1)) - (1ll << 28);
+    if (low <= 256 && low >= -256) return __double2float_rn(__ddiv_rn(d, p0));
+    return __double2float_rn(g1);
+}
+
+// Sum of non-negative floats as an exact 192-bit fixed-point number in units of
+// 2^-96 (terms below 2^-73 lose their lowest bits; such squares need
+// |alpha| < 2^-36).  Integer addition makes the result independent of order.
+struct U192 {
+    uint64_t w0, w1, w2;
+};
+
+__device__ __forceinline__ void u192_add(U192 &a, uint64_t p0, uint64_t p1, uint64_t p2) {
+    asm("add.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, %4;\n\taddc.u64 %2, %2, %5;"
+        : "+l"(a.w0), "+l"(a.w1), "+l"(a.w2)
+        : "l"(p0), "l"(p1), "l"(p2));
+}
+
+// Adds a finite square; returns false for a square too large to hold (>= 2^72).
+__device__ __forceinline__ bool u192_add_float(U192 &a, float v) {
+    const uint32_t bits = __float_as_uint(v);
+    const uint32_t e = bits >> 23;
+    uint64_t m = e ? ((bits & 0x7fffffu) | 0x800000u) : (bits & 0x7fffffu);
+    if (m == 0) return true;
+    int sh = (e ? (int)e : 1) - 150 + 96;  // bit position of m's lowest bit
+    if (sh < 0) {
+        if (sh <= -24) return true;
+        m >>= -sh;
+        sh = 0;
+    }
+    uint64_t p0 = 0, p1 = 0, p2 = 0;
+    if (sh < 64) {
+        p0 = m << sh;
+        p1 = sh ? (m >> (64 - sh)) : 0;
+    } else if (sh < 128) {
+        const int t = sh - 64;
+        p1 = m << t;
+        p2 = t ? (m >> (64 - t)) : 0;
+    } else if (sh <= 192 - 24) {
+        p2 = m << (sh - 128);
+    } else {
+        return false;
+    }
+    u192_add(a, p0, p1, p2);
+    return true;
+}
+
+__device__ __forceinline__ U192 u192_shfl_down(const U192 &a, int d) {
+    U192 r;
+    r.w0 = __shfl_down_sync(0xffffffffu, a.w0, d);
+    r.w1 = __shfl_down_sync(0xffffffffu, a.w1, d);
+    r.w2 = __shfl_down_sync(0xffffffffu, a.w2, d);
+    return r;
+}
+
+// value * 2^-96 rounded to nearest-even double
+__device__ double u192_to_double(const U192 &a) {
+    uint64_t top, next, rest;
+    int base;
+    if (a.w2) { top = a.w2; next = a.w1; rest = a.w0; base = 128; }
+    else if (a.w1) { top = a.w1; next = a.w0; rest = 0; base = 64; }
+    else if (a.w0) { top = a.w0; next = 0; rest = 0; base = 0; }
+    else return 0.0;
+    const int lz = __clzll(top);
+    int pos = base + 63 - lz;  // index of the most significant bit
+    const uint64_t hi64 = lz ? ((top << lz) | (next >> (64 - lz))) : top;
+    const uint64_t below = lz ? (next << lz) : next;
+    uint64_t mant = hi64 >> 11;
+    const bool round_bit = (hi64 >> 10) & 1;
+    const bool sticky = (hi64 & 0x3ffull) || below || rest;
+    if (round_bit && (sticky || (mant & 1))) {
+        mant++;
+        if (mant == (1ull << 53)) {
+            mant >>= 1;
+            pos++;
+        }
+    }
+    return ldexp((double)mant, pos - 52 - 96);
+}
+
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
+
+// prob[p][0][c] = c/n0, [1][c] = c/n1, [2][c] = c/n2, [3][c] = 1/(c/n2): the
+// exact IEEE quotients the reference forms for count c.  grid = (PROB_TABLE/256, B)
+__global__ void k_tables(BuildArgs a) {
+    const int p = blockIdx.y;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= PROB_TABLE) return;
+    const double n0 = (double)a.tot[p * 4 + 0], n1 = (double)a.tot[p * 4 + 1],
+                 n2 = (double)a.tot[p * 4 + 2];
+    double *t = a.prob + (uint64_t)p * 4 * PROB_TABLE;
+    const double pm = __ddiv_rn((double)c, n2);
+    t[c] = __ddiv_rn((double)c, n0);
+    t[PROB_TABLE + c] = __ddiv_rn((double)c, n1);
+    t[2 * PROB_TABLE + c] = pm;
+    t[3 * PROB_TABLE + c] = __ddiv_rn(1.0, pm);
+}
 
 // tile_base[p] = number of TILE-sized tiles of proteomes < p; tile_base[B] = total.
 __global__ void k_prep(int B, const uint64_t *__restrict__ seq_off, uint64_t *tile_base) {
@@ -158,7 +287,7 @@ __device__ __forceinline__ uint32_t cand_count_of(const BuildArgs &a, int p, uin
     if (q >= a.T1) return 0;
     uint32_t c = a.c1[(uint64_t)p * a.T1 + q];
     if (!c) return 0;
-    return __popc(a.mask[(uint64_t)p * a.T2 + (q % a.T2)]);
+    return __popc(a.mask[(uint64_t)p * a.T2 + a.fdT2.mod((uint32_t)q)]);
 }
 
 // Candidates per chunk of CH (K-1)-mers.  grid = (NCH, B)
@@ -250,7 +379,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
                     uint32_t b = dig[li + K - 1];
                     if (b != 0xffu) {
                         v0 = true;
-                        uint32_t m = w % (uint32_t)a.T2;
+                        uint32_t m = a.fdT2.mod(w);
                         slot = cbase + coff[w] + __popc(mk[m] & ((1u << b) - 1u));
                     }
                 }
@@ -289,8 +418,9 @@ __device__ __forceinline__ void locate(const uint32_t *sm_off, uint32_t nq, uint
 // grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     __shared__ uint32_t sm_off[CH];
-    __shared__ double s_hi[CHUNK_THREADS / 32], s_lo[CHUNK_THREADS / 32];
-    __shared__ uint32_t s_surv[CHUNK_THREADS / 32], s_m1[CHUNK_THREADS / 32];
+    __shared__ U192 s_norm[CHUNK_THREADS / 32];
+    __shared__ uint32_t s_surv[CHUNK_THREADS / 32], s_m1[CHUNK_THREADS / 32],
+        s_bad[CHUNK_THREADS / 32];
     const int p = blockIdx.y, c = blockIdx.x;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
     const uint64_t cb = a.chunk_cand_off[pc];
@@ -301,92 +431,100 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1;
     const uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
     const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+    const double *prob = a.prob + (uint64_t)p * 4 * PROB_TABLE;
     const uint32_t n0 = a.tot[p * 4 + 0], n1 = a.tot[p * 4 + 1], n2 = a.tot[p * 4 + 2];
     uint32_t local0 = ncand ? coff[q0] : 0;
     for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
     __syncthreads();
-    DD acc = {0.0, 0.0};
-    uint32_t surv = 0, m1 = 0;
+    U192 acc = {0, 0, 0};
+    uint32_t surv = 0, m1 = 0, bad = 0;
     const uint32_t A = a.A;
     for (uint32_t u = threadIdx.x; u < ncand; u += CHUNK_THREADS) {
         if (cb + u >= a.cand_cap) break;
         uint32_t ql, r;
         locate(sm_off, nq, u, ql, r);
-        const uint64_t q = q0 + ql;
-        const uint32_t m = (uint32_t)(q % a.T2);
+        const uint32_t q = (uint32_t)(q0 + ql);
+        const uint32_t m = a.fdT2.mod(q);
         const uint32_t b = nth_set_bit(mk[m], r);
         const uint32_t full = a.c0a[cb + u];
         const uint32_t pre = c1[q];
-        const uint32_t suf = c1[(uint64_t)m * A + b];
+        const uint32_t suf = c1[m * A + b];
         const uint32_t mid = c2[m];
-        const float f = markov_alpha(full, pre, suf, mid, n0, n1, n2);
+        const float f = markov_alpha_fast(full, pre, suf, mid, n0, n1, n2, prob);
         const uint32_t bits = __float_as_uint(f);
         a.c0a[cb + u] = bits;
         if (bits != 0u) {
             surv++;
-            const float sq = __fmul_rn(f, f);
+            const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
             if (sq == 1.0f) m1++;
-            else dd_add(acc, (double)sq);
+            else if (isnan(sq)) bad |= 1u;
+            else if (isinf(sq) || !u192_add_float(acc, sq)) bad |= 2u;
         }
     }
-    // reduce
+    // reduce (integer: exact and order independent)
     surv = __reduce_add_sync(0xffffffffu, surv);
     m1 = __reduce_add_sync(0xffffffffu, m1);
+    bad = __reduce_or_sync(0xffffffffu, bad);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        DD o;
-        o.hi = __shfl_down_sync(0xffffffffu, acc.hi, d);
-        o.lo = __shfl_down_sync(0xffffffffu, acc.lo, d);
-        acc = dd_merge(acc, o);
+        const U192 o = u192_shfl_down(acc, d);
+        u192_add(acc, o.w0, o.w1, o.w2);
     }
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        s_hi[w] = acc.hi; s_lo[w] = acc.lo; s_surv[w] = surv; s_m1[w] = m1;
+        s_norm[w] = acc; s_surv[w] = surv; s_m1[w] = m1; s_bad[w] = bad;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        DD t = {0.0, 0.0};
-        uint32_t ts = 0, tm = 0;
+        U192 t = {0, 0, 0};
+        uint32_t ts = 0, tm = 0, tb = 0;
         for (int i = 0; i < CHUNK_THREADS / 32; i++) {
-            t = dd_merge(t, DD{s_hi[i], s_lo[i]});
+            u192_add(t, s_norm[i].w0, s_norm[i].w1, s_norm[i].w2);
             ts += s_surv[i];
             tm += s_m1[i];
+            tb |= s_bad[i];
         }
         a.chunk_surv[pc] = ts;
         a.chunk_m1[pc] = tm;
-        a.chunk_nhi[pc] = t.hi;
-        a.chunk_nlo[pc] = t.lo;
+        a.chunk_bad[pc] = tb;
+        a.chunk_norm[3 * pc + 0] = t.w0;
+        a.chunk_norm[3 * pc + 1] = t.w1;
+        a.chunk_norm[3 * pc + 2] = t.w2;
     }
 }
 
-// Per proteome: norm (fixed chunk order), scale = sqrt(norm), nnz.  grid = B, 32 threads.
+// Per proteome: norm = exact sum of the squares rounded once to double
+// (native.cu:415-428 sums the same float squares in double, in CUB's order),
+// scale = sqrt(norm), its reciprocal, nnz.  grid = B, 32 threads.
 __global__ void k_norm(BuildArgs a) {
     const int p = blockIdx.x;
     const int lane = threadIdx.x;
-    DD acc = {0.0, 0.0};
+    U192 acc = {0, 0, 0};
     uint64_t m1 = 0;
+    uint32_t bad = 0;
     for (uint64_t c = lane; c < a.NCH; c += 32) {
         const uint64_t pc = (uint64_t)p * a.NCH + c;
-        acc = dd_merge(acc, DD{a.chunk_nhi[pc], a.chunk_nlo[pc]});
+        u192_add(acc, a.chunk_norm[3 * pc], a.chunk_norm[3 * pc + 1], a.chunk_norm[3 * pc + 2]);
         m1 += a.chunk_m1[pc];
+        bad |= a.chunk_bad[pc];
     }
-    // fixed-order tree over lanes
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        DD o;
-        o.hi = __shfl_down_sync(0xffffffffu, acc.hi, d);
-        o.lo = __shfl_down_sync(0xffffffffu, acc.lo, d);
-        acc = dd_merge(acc, o);
+        const U192 o = u192_shfl_down(acc, d);
+        u192_add(acc, o.w0, o.w1, o.w2);
         m1 += __shfl_down_sync(0xffffffffu, m1, d);
     }
+    bad = __reduce_or_sync(0xffffffffu, bad);
     if (lane == 0) {
-        // exact integer count of unit squares, then the rest
-        DD n = {(double)m1, 0.0};
-        n = dd_merge(n, acc);
-        const double norm = __dadd_rn(n.hi, n.lo);
+        // each unit square adds 1.0 = 2^96 units: bit 32 of the middle word
+        u192_add(acc, 0, m1 << 32, m1 >> 32);
+        double norm = u192_to_double(acc);
+        if (bad & 1u) norm = __longlong_as_double(0x7ff8000000000000ll);
+        else if (bad & 2u) norm = __longlong_as_double(0x7ff0000000000000ll);
         const double scale = __dsqrt_rn(norm);
         a.norm[p] = norm;
         a.scale[p] = scale;
+        a.rscale[p] = __ddiv_rn(1.0, scale);
         const uint64_t o0 = a.chunk_out_off[(uint64_t)p * a.NCH];
         const uint64_t o1 = a.chunk_out_off[(uint64_t)(p + 1) * a.NCH];
         a.nnz[p] = o1 - o0;
@@ -394,8 +532,10 @@ __global__ void k_norm(BuildArgs a) {
     }
 }
 
-// Writes survivors in candidate (= key) order: keys and float(alpha / scale).
-// grid = (NCH, B)
+// Writes survivors in candidate (= key) order: keys and float(alpha / scale)
+// (native.cu:460-468).  The division by the per-proteome constant scale uses
+// its correctly rounded reciprocal and one FMA correction (Markstein), which
+// yields the correctly rounded double quotient.  grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
     __shared__ uint32_t sm_off[CH];
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
@@ -412,7 +552,9 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
     for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
     __syncthreads();
     const double scale = a.scale[p];
-    const float vm1 = __double2float_rn(__ddiv_rn(-1.0, scale));
+    const double rs = a.rscale[p];
+    const bool finite = isfinite(scale) && scale > 0.0;
+    const float vm1 = __double2float_rn(-rs);  // RN(-1/scale) == -RN(1/scale)
     // destination: proteome base in the caller's arena + offset within proteome
     const uint64_t pbase = a.chunk_out_off[(uint64_t)p * a.NCH];
     uint64_t dst = a.dst_base[p] + (a.chunk_out_off[pc] - pbase);
@@ -427,9 +569,9 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
             if (bits) {
                 uint32_t ql, r;
                 locate(sm_off, nq, u, ql, r);
-                const uint64_t q = q0 + ql;
-                const uint32_t m = (uint32_t)(q % a.T2);
-                key = (uint32_t)(q * A + nth_set_bit(mk[m], r));
+                const uint32_t q = (uint32_t)(q0 + ql);
+                const uint32_t m = a.fdT2.mod(q);
+                key = q * A + nth_set_bit(mk[m], r);
             }
         }
         uint64_t tot;
@@ -438,8 +580,18 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
             const uint64_t o = dst + rank;
             if (o < dst_end) {
                 const float f = __uint_as_float(bits);
+                float v;
+                if (!finite || !isfinite(f)) {
+                    v = __double2float_rn(__ddiv_rn((double)f, scale));
+                } else if (f == -1.0f) {
+                    v = vm1;
+                } else {
+                    const double x = (double)f;
+                    const double q = __dmul_rn(x, rs);
+                    v = __double2float_rn(__fma_rn(__fma_rn(-q, scale, x), rs, q));
+                }
                 a.out_keys[o] = key;
-                a.out_vals[o] = (f == -1.0f) ? vm1 : __double2float_rn(__ddiv_rn((double)f, scale));
+                a.out_vals[o] = v;
             }
         }
         dst += tot;
@@ -479,11 +631,13 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     s += scratch_bytes<uint32_t>(nc);              // chunk_surv
     s += scratch_bytes<uint64_t>(nc + 1);          // chunk_out_off
     s += scratch_bytes<uint32_t>(nc);              // chunk_m1
-    s += scratch_bytes<double>(nc);                // chunk_nhi
-    s += scratch_bytes<double>(nc);                // chunk_nlo
+    s += scratch_bytes<uint64_t>(3 * nc);          // chunk_norm
+    s += scratch_bytes<uint32_t>(nc);              // chunk_bad
+    s += scratch_bytes<double>(4 * (uint64_t)PROB_TABLE * B);  // prob tables
     s += scratch_bytes<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);  // scan temp
     s += scratch_bytes<double>(B);                 // norm
     s += scratch_bytes<double>(B);                 // scale
+    s += scratch_bytes<double>(B);                 // rscale
     s += scratch_bytes<uint64_t>(B);               // nnz
     s += scratch_bytes<uint64_t>(B);               // out_base
     s += scratch_bytes<uint64_t>(B);               // dst_base
@@ -511,11 +665,14 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.chunk_surv = sc.take<uint32_t>(nc);
     r.chunk_out_off = sc.take<uint64_t>(nc + 1);
     r.chunk_m1 = sc.take<uint32_t>(nc);
-    r.chunk_nhi = sc.take<double>(nc);
-    r.chunk_nlo = sc.take<double>(nc);
+    r.chunk_norm = sc.take<uint64_t>(3 * nc);
+    r.chunk_bad = sc.take<uint32_t>(nc);
+    r.prob = sc.take<double>(4 * (uint64_t)PROB_TABLE * B);
+    r.fdT2.set((uint32_t)g.T2);
     r.scan_tmp = sc.take<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);
     r.norm = sc.take<double>(B);
     r.scale = sc.take<double>(B);
+    r.rscale = sc.take<double>(B);
     r.nnz = sc.take<uint64_t>(B);
     r.out_base = sc.take<uint64_t>(B);
     r.dst_base = sc.take<uint64_t>(B);
@@ -550,6 +707,7 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     k_prep<<<1, 32, 0, st>>>(a.B, a.seq_off, a.tile_base);
     const int grid_seq = sm_count() * 8;
     k_count<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
+    k_tables<<<dim3(PROB_TABLE / 256, a.B), 256, 0, st>>>(a);
     dim3 gch((unsigned)a.NCH, (unsigned)a.B);
     k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
@@ -570,9 +728,10 @@ cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
 }
 
 // Kernel counting per launch of build_plan + build_emit (for launch accounting).
-// Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_cand_count,
-// scan (3), k_cand_offsets, k_c0_zero, k_c0_scatter, k_alpha, scan (3), k_norm;
-// emit k_arena_offsets, k_compact, k_arena_pad.  (Five memsets are not counted.)
-int build_launches_per_batch() { return 14 + 3; }
+// Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_tables,
+// k_cand_count, scan (3), k_cand_offsets, k_c0_zero, k_c0_scatter, k_alpha,
+// scan (3), k_norm; emit k_arena_offsets, k_compact, k_arena_pad.  (Five
+// memsets are not counted.)
+int build_launches_per_batch() { return 15 + 3; }
 
 }  // namespace phylo

@@ -11,6 +11,22 @@ struct BuildGeometry {
     uint64_t NCH;    // chunks of (K-1)-mers per proteome
 };
 
+// Division by a run-time constant d (2 <= d < 2^32) for 32-bit numerators:
+// q / d == floor(q * M / 2^64) with M = ceil(2^64 / d).
+struct FastDiv {
+    uint64_t M;
+    uint32_t d;
+    __host__ void set(uint32_t divisor) {
+        d = divisor;
+        M = ~0ull / divisor + 1;  // ceil(2^64 / d) for d not a power of two; exact otherwise
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t q) const { return (uint32_t)__umul64hi(q, M); }
+    __device__ __forceinline__ uint32_t mod(uint32_t q) const { return q - div(q) * d; }
+};
+
+// Count -> probability tables are kept for counts below this bound.
+constexpr int PROB_TABLE = 4096;
+
 // Everything a build launch needs; plain device pointers, passed by value.
 struct BuildArgs {
     int alpha, k, B;
@@ -31,10 +47,13 @@ struct BuildArgs {
     uint32_t *chunk_surv;     // survivors per chunk
     uint64_t *chunk_out_off;  // exclusive scan, [nc+1]
     uint32_t *chunk_m1;       // survivors with alpha^2 == 1
-    double *chunk_nhi, *chunk_nlo;
+    uint64_t *chunk_norm;     // [nc][3]: sum of the other alpha^2 as 192-bit fixed point, 2^-96 units
+    uint32_t *chunk_bad;      // [nc]: bit 0 a NaN square, bit 1 an infinite one
+    double *prob;             // [B][4][PROB_TABLE]: c/n0, c/n1, c/n2, 1/(c/n2)
+    FastDiv fdT2;             // division by A^(K-2)
     uint64_t *scan_tmp;
     // per proteome results
-    double *norm, *scale;
+    double *norm, *scale, *rscale;  // sum alpha^2, sqrt of it, RN(1/sqrt)
     uint64_t *nnz, *out_base;
     uint64_t *dst_base, *dst_cap;  // where k_compact writes proteome p
     uint32_t *status;

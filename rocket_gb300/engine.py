@@ -9,7 +9,7 @@ correlateGPU for every pair; rocket/scheduler/DeviceWorker.java:118-323):
   pair kernel can read them with 16-byte loads.
 * :class:`PairEngine` compares every pair of an arena (or a rectangle of row
   and column vectors) with the window-tiled kernel of csrc/allpairs.cu.  The
-  planner sorts vectors by size, cuts the pair matrix into 16 x 256 tiles and
+  planner sorts vectors by size, cuts the pair matrix into 16 x 64 tiles and
   the key space into segments, estimates each item's cost and hands items out
   longest first.
 
@@ -30,7 +30,7 @@ from . import _native
 from ._native import check
 
 AP_TI = 16
-AP_TJ = 256
+AP_TJ = 64
 NSYM = {"protein": 21, "DNA": 4}
 
 
@@ -231,6 +231,8 @@ class EngineConfig:
     fold: int = 16
     items_per_cta: int = 4
     min_windows_per_item: int = 64
+    segments: int = 0        # key segments per tile; 0 = chosen from the plan size.  A fixed
+                             # value makes each pair's arithmetic independent of the plan.
 
 
 class PairEngine:
@@ -249,6 +251,7 @@ class PairEngine:
         self.part = None
         self.launches = 0
         self.cmp_scratch = None
+        self.self_part = None
 
     # -- window index ------------------------------------------------------
     def ensure_index(self, stream=None) -> None:
@@ -264,30 +267,35 @@ class PairEngine:
             new[:a.roff.shape[0]].copy_(a.roff)
             a.roff = new
         if a.indexed < a.n:
+            maxlen = int(np.max(np.diff(a.off[a.indexed:a.n + 1])))
             check(self.L.phyloWindowIndex(
                 _stream_handle(stream), _p(a.keys), _p(a.vec_off[a.indexed:]), a.n - a.indexed,
-                self.cfg.wshift, R, _p(a.roff[a.indexed])))
+                self.cfg.wshift, R, maxlen, _p(a.roff[a.indexed])))
             self.launches += 1
             a.indexed = a.n
 
     # -- planning ------------------------------------------------------------
     def _segments(self, ntiles: int) -> int:
+        if self.cfg.segments > 0:
+            return int(min(self.cfg.segments, max(1, self.arena.R)))
         target = self.cfg.items_per_cta * self.grid
         S = max(1, math.ceil(target / max(ntiles, 1)))
         return int(max(1, min(S, self.arena.R // self.cfg.min_windows_per_item)))
 
-    def _finish_plan(self, rowids, colids, tiles, upper, mirror, ldc, pairs) -> PairPlan:
+    def _finish_plan(self, rowids, colids, tiles, upper, mirror, ldc, pairs,
+                     row_nnz=None, col_nnz=None) -> PairPlan:
         a = self.arena
         ntiles = len(tiles)
         S = self._segments(ntiles)
         R = a.R
-        nnz = a.nnz
+        row_nnz = a.nnz if row_nnz is None else row_nnz
+        col_nnz = a.nnz if col_nnz is None else col_nnz
         items = np.zeros((ntiles * S, 8), np.int64)
         est = np.zeros(ntiles * S)
         estp = np.zeros(ntiles * S)
         for t, (r0, nr, c0, nc) in enumerate(tiles):
-            rn = nnz[rowids[r0:r0 + nr]]
-            cn = nnz[colids[c0:c0 + nc]]
+            rn = row_nnz[rowids[r0:r0 + nr]]
+            cn = col_nnz[colids[c0:c0 + nc]]
             # linear model: 16 products per column entry + row scatter/clear
             # + a fixed cost per window
             e_tile = AP_TI * cn.sum() + 2.0 * rn.sum() + 64.0 * R
@@ -328,19 +336,23 @@ class PairEngine:
                 c += nc
         return self._finish_plan(perm, perm, tiles, True, True, ldc or a.n, N * (N - 1) // 2)
 
-    def plan_rect(self, row_ids: Sequence[int], col_ids: Sequence[int], ldc: int) -> PairPlan:
-        """Every (row, column) pair; out[row_id * ldc + col_id]."""
+    def plan_rect(self, row_ids: Sequence[int], col_ids: Sequence[int], ldc: int,
+                  col_arena: Optional[Arena] = None) -> PairPlan:
+        """Every (row, column) pair; out[row_id * ldc + col_id].  Rows are vectors
+        of this engine's arena, columns of ``col_arena`` (default: the same)."""
         a = self.arena
+        ca = col_arena if col_arena is not None else a
         rows = np.asarray(row_ids, np.int64)
         cols = np.asarray(col_ids, np.int64)
         rows = rows[np.argsort(-a.nnz[rows], kind="stable")]
-        cols = cols[np.argsort(-a.nnz[cols], kind="stable")]
+        cols = cols[np.argsort(-ca.nnz[cols], kind="stable")]
         tiles = []
         for r0 in range(0, len(rows), AP_TI):
             nr = min(AP_TI, len(rows) - r0)
             for c0 in range(0, len(cols), AP_TJ):
                 tiles.append((r0, nr, c0, min(AP_TJ, len(cols) - c0)))
-        return self._finish_plan(rows, cols, tiles, False, False, ldc, len(rows) * len(cols))
+        return self._finish_plan(rows, cols, tiles, False, False, ldc, len(rows) * len(cols),
+                                 a.nnz, ca.nnz)
 
     # -- execution -------------------------------------------------------------
     def _parts(self, plan: PairPlan) -> torch.Tensor:
@@ -350,7 +362,7 @@ class PairEngine:
         return self.part
 
     def run(self, plan: PairPlan, out: torch.Tensor, stream=None, item_cycles: torch.Tensor = None,
-            diagonal: bool = True, events=None) -> None:
+            diagonal: bool = True, events=None, col_arena: Optional[Arena] = None) -> None:
         """Writes C of every planned pair into ``out`` (float64, row-major, ldc).
         ``events`` = (start, end) CUDA events recorded around the pair kernel."""
         a = self.arena
@@ -361,8 +373,10 @@ class PairEngine:
             self.counter.zero_()
         if events is not None:
             events[0].record(s_obj)
+        ca = col_arena if col_arena is not None else a
         check(self.L.phyloPairsLaunch(
-            st, _p(a.keys), _p(a.values), _p(a.vec_off), _p(a.roff), a.R, self.cfg.wshift,
+            st, _p(a.keys), _p(a.values), _p(a.vec_off), _p(a.roff), _p(ca.keys), _p(ca.values),
+            _p(ca.vec_off), _p(ca.roff), a.R, self.cfg.wshift,
             _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems, _p(self.counter),
             _p(part), self.cfg.fold, _p(item_cycles) if item_cycles is not None else 0,
             self.grid))
@@ -373,39 +387,51 @@ class PairEngine:
             _p(out), plan.ldc, int(plan.upper), int(plan.mirror)))
         self.launches += 3  # counter fill, pair kernel, reduction
         if diagonal and plan.upper:
-            check(self.L.phyloSelfDot(st, _p(a.values), _p(a.vec_off), a.n, _p(out), plan.ldc))
-            self.launches += 1
-        self._fix_nonfinite(plan, out, s_obj)
+            maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
+            nb = int(self.L.phyloSelfDotPartBytes(a.n, maxlen))
+            if self.self_part is None or self.self_part.numel() < nb:
+                self.self_part = torch.empty(max(nb, 8), dtype=torch.uint8, device=self.device)
+            check(self.L.phyloSelfDot(st, _p(a.values), _p(a.vec_off), a.n, maxlen,
+                                      _p(self.self_part), _p(out), plan.ldc))
+            self.launches += 2
+        self._fix_nonfinite(plan, out, s_obj, col_arena)
 
-    def _fix_nonfinite(self, plan: PairPlan, out: torch.Tensor, stream) -> None:
+    def _fix_nonfinite(self, plan: PairPlan, out: torch.Tensor, stream,
+                       col_arena: Optional[Arena] = None) -> None:
         """Vectors whose values are NaN/inf: recompute their pairs with the
         merge-path kernel, which only multiplies values of shared keys (as the
         reference does)."""
-        a = self.arena
-        bad = np.flatnonzero(~np.isfinite(a.norms[:a.n]))
-        if len(bad) == 0:
+        ra = self.arena
+        ca = col_arena if col_arena is not None else ra
+        bad_r = set(np.flatnonzero(~np.isfinite(ra.norms[:ra.n])).tolist())
+        bad_c = set(np.flatnonzero(~np.isfinite(ca.norms[:ca.n])).tolist())
+        if not bad_r and not bad_c:
             return
         st = _stream_handle(stream)
-        maxn = int(a.nnz.max())
         if self.cmp_scratch is None:
-            n = int(self.L.estimateScratchMemory(a.alphabet.encode(), 3, maxn))
+            maxn = int(max(ra.nnz.max(), ca.nnz.max()))
+            n = int(self.L.estimateScratchMemory(ra.alphabet.encode(), 3, maxn))
             self.cmp_scratch = torch.empty(n, dtype=torch.uint8, device=self.device)
         rows = plan.rowids.cpu().numpy()
         cols = plan.colids.cpu().numpy()
-        ks, vs = a.keys, a.values
-        for r in rows:
-            for c in cols:
-                if r == c or not (r in bad or c in bad):
-                    continue
-                if plan.upper and not (np.flatnonzero(rows == r)[0] < np.flatnonzero(cols == c)[0]):
-                    continue
-                o = out.view(-1)[int(r) * plan.ldc + int(c):]
-                check(self.L.phyloComparePairAsync(
-                    st, _p(self.cmp_scratch), self.cmp_scratch.numel(), _p(ks[a.off[r]:]),
-                    _p(vs[a.off[r]:]), int(a.nnz[r]), _p(ks[a.off[c]:]), _p(vs[a.off[c]:]),
-                    int(a.nnz[c]), _p(o)))
-                if plan.mirror:
-                    out.view(-1)[int(c) * plan.ldc + int(r)] = out.view(-1)[int(r) * plan.ldc + int(c)]
+        flat = out.view(-1)
+        for ti in range(plan.ntiles):
+            r0, nr, c0, nc = (int(x) for x in plan.tiles[ti].cpu().numpy())
+            for i in range(r0, r0 + nr):
+                for j in range(c0, c0 + nc):
+                    r, c = int(rows[i]), int(cols[j])
+                    if plan.upper and not i < j:
+                        continue
+                    if r not in bad_r and c not in bad_c:
+                        continue
+                    o = flat[r * plan.ldc + c:]
+                    check(self.L.phyloComparePairAsync(
+                        st, _p(self.cmp_scratch), self.cmp_scratch.numel(),
+                        _p(ra.keys[int(ra.off[r]):]), _p(ra.values[int(ra.off[r]):]),
+                        int(ra.nnz[r]), _p(ca.keys[int(ca.off[c]):]),
+                        _p(ca.values[int(ca.off[c]):]), int(ca.nnz[c]), _p(o)))
+                    if plan.mirror:
+                        flat[c * plan.ldc + r] = flat[r * plan.ldc + c]
 
 
 def distances(c: torch.Tensor) -> torch.Tensor:
