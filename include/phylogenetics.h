@@ -183,6 +183,20 @@ int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int 
 /* Scratch bytes phyloSelfDot needs. */
 long phyloSelfDotPartBytes(int num_vectors, long max_vector_len);
 
+/* Scratch bytes of phyloComparePairsMany for num_pairs pairs and at most
+ * max_tiles merge tiles (sum over pairs of ceil((nl + nr) / 4096)). */
+long phyloComparePairsManyScratch(int num_pairs, long max_tiles);
+
+/* C of many pairs with the merge-path kernels in one launch sequence: pair p
+ * compares vector d_pa[p] of the left arena with vector d_pb[p] of the right
+ * arena (arena = keys, values, uint64 offsets, uint32 sizes); d_out[p] gets C
+ * (double).  Asynchronous. */
+int phyloComparePairsMany(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                          uintptr_t d_lkeys, uintptr_t d_lvalues, uintptr_t d_loff,
+                          uintptr_t d_lnnz, uintptr_t d_rkeys, uintptr_t d_rvalues,
+                          uintptr_t d_roff, uintptr_t d_rnnz, uintptr_t d_pa, uintptr_t d_pb,
+                          int num_pairs, long max_tiles, uintptr_t d_out);
+
 /* compareCompositionVectors without the synchronisation (result left on the
  * device); scratch from estimateScratchMemory. */
 int phyloComparePairAsync(uintptr_t stream, uintptr_t d_scratch, long scratch_size,

@@ -100,6 +100,10 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloComparePairAsync.argtypes = [c_ptr, c_ptr, c_long, c_ptr, c_ptr, c_int, c_ptr, c_ptr,
                                         c_int, c_ptr]
     L.phyloComparePairAsync.restype = c_int
+    L.phyloComparePairsManyScratch.argtypes = [c_int, c_long]
+    L.phyloComparePairsManyScratch.restype = c_long
+    L.phyloComparePairsMany.argtypes = [c_ptr, c_ptr, c_long] + [c_ptr] * 10 + [c_int, c_long, c_ptr]
+    L.phyloComparePairsMany.restype = c_int
 
 
 # Every symbol that include/phylogenetics.h declares.
@@ -108,7 +112,8 @@ EXPORTED = [
     "compareCompositionVectorsStatic", "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchEmit", "phyloBuildBatchNorms",
     "phyloBuildBatchCounts", "phyloBuildLaunchesPerBatch", "phyloWindowIndex",
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsLaunch", "phyloPairsReduce",
-    "phyloSelfDot", "phyloSelfDotPartBytes", "phyloComparePairAsync",
+    "phyloSelfDot", "phyloSelfDotPartBytes", "phyloComparePairsManyScratch",
+    "phyloComparePairsMany", "phyloComparePairAsync",
 ]
 
 

@@ -9,14 +9,15 @@
 //     roff[v][r] (the multi-way analogue of a merge-path split: the position of
 //     key r*W in every sorted list, found once per vector) gives each vector's
 //     sub-list in every window.
-//   * A work item is 16 row vectors x up to 256 column vectors x a run of
+//   * A work item is 16 row vectors x up to 64 column vectors x a run of
 //     windows.  For each window the 16 row sub-lists are scattered into a
-//     shared-memory table D[key - r*W][row] (16 floats per key, float4 chunks
-//     XOR-swizzled so random gathers spread over the banks; one extra zero row
-//     serves masked lanes).  Each thread owns one column vector and streams its
-//     sub-list with 16-byte loads; every entry (key, b) adds D[key][i] * b to
-//     16 accumulators -- one per row.  Keys absent from a row read 0, so the
-//     sum over the column's entries is exactly the intersection sum.
+//     shared-memory table D[key - r*W] of 80-byte records (16 row values +
+//     padding: the odd stride spreads random gathers over the banks; one extra
+//     zero record serves masked lanes).  Four lanes share a column vector and
+//     stream its sub-list in 16-byte groups through a cp.async ring; every entry
+//     (key, b) adds D[key][i] * b to 16 accumulators -- one per row.  Keys
+//     absent from a row read 0, so the column's sum is exactly the
+//     intersection sum.
 //   * Accumulation: FP32 products summed in FP32 for at most `fold` products,
 //     then folded into a float-float (TwoSum) accumulator.  Bound on the error
 //     of C: (fold + 2) * 2^-24 * sum|a*b| <= (fold + 2) * 2^-24 for unit
@@ -25,30 +26,36 @@
 //     order given (the host sorts them by estimated cost, longest first).
 //     Several CTAs share an SM, so one CTA's window barriers overlap another's
 //     work.
-//   * Each item writes a 16 x 256 float-float partial block; ap_reduce sums the
+//   * Each item writes a 16 x 64 float-float partial block; ap_reduce sums the
 //     blocks of a tile in a fixed order (double-double), so results do not
 //     depend on scheduling.
 #include "allpairs.cuh"
 
 namespace phylo {
 
+// The row table D holds, for each key of the window, the 16 row values in one
+// 80-byte record (64 bytes of values + 16 bytes of padding).  The odd stride
+// (5 x 16 bytes) spreads the four 16-byte loads of random keys over all eight
+// 16-byte bank groups, and the four loads of a key are one base address plus
+// constant offsets.  One extra record (index W) stays zero for masked lanes.
+constexpr uint32_t D_STRIDE = 20;  // floats per key record
+
 size_t ap_ring_bytes();
 size_t ap_smem_bytes(uint32_t wshift) {
-    return (((size_t)1 << wshift) + 1) * AP_TI * sizeof(float) + ap_ring_bytes();
+    return (((size_t)1 << wshift) + 1) * D_STRIDE * sizeof(float) + ap_ring_bytes();
 }
 
 int ap_max_wshift() { return 11; }
 
 // float index of (key idx, row) in D
 __device__ __forceinline__ uint32_t d_slot(uint32_t idx, uint32_t row) {
-    return idx * 16u + ((((row >> 2) ^ (idx >> 1)) & 3u) << 2) + (row & 3u);
+    return idx * D_STRIDE + row;
 }
 
 __device__ __forceinline__ void fma_entry(const float *__restrict__ D, uint32_t idx, float b,
                                           float (&acc)[16]) {
-    const float4 *rowp = reinterpret_cast<const float4 *>(D + idx * 16u);
-    const uint32_t sw = (idx >> 1) & 3u;
-    const float4 q0 = rowp[0 ^ sw], q1 = rowp[1 ^ sw], q2 = rowp[2 ^ sw], q3 = rowp[3 ^ sw];
+    const float4 *rowp = reinterpret_cast<const float4 *>(D + idx * D_STRIDE);
+    const float4 q0 = rowp[0], q1 = rowp[1], q2 = rowp[2], q3 = rowp[3];
     acc[0] = __fmaf_rn(q0.x, b, acc[0]);
     acc[1] = __fmaf_rn(q0.y, b, acc[1]);
     acc[2] = __fmaf_rn(q0.z, b, acc[2]);
@@ -81,7 +88,7 @@ __device__ __forceinline__ void fold16(float (&acc)[16], float (&hi)[16], float 
 // Per-thread ring of 16-byte column groups (4 keys + 4 values) fetched with
 // cp.async, RING groups ahead of the one being used, so a thread's column stream
 // stays in flight across window barriers.
-constexpr int RING = 4;
+constexpr int RING = 2;
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem)
@@ -111,14 +118,14 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t W = 1u << a.wshift, wmask = W - 1u;
     float *D = reinterpret_cast<float *>(smem);                    // (W + 1) x 16
-    uint4 *ring_k = reinterpret_cast<uint4 *>(smem + (size_t)(W + 1) * 64);
+    uint4 *ring_k = reinterpret_cast<uint4 *>(smem + (size_t)(W + 1) * D_STRIDE * 4);
     float4 *ring_v = reinterpret_cast<float4 *>(ring_k + RING * AP_THREADS);
     __shared__ uint32_t s_item;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t jcol = threadIdx.x / AP_LPC, q = threadIdx.x % AP_LPC;
     const uint32_t Rs = a.R + 1;
 
-    for (uint32_t i = threadIdx.x; i < (W + 1) * 4u; i += AP_THREADS)
+    for (uint32_t i = threadIdx.x; i < (W + 1) * (D_STRIDE / 4); i += AP_THREADS)
         reinterpret_cast<float4 *>(D)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 
     for (;;) {

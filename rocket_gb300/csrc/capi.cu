@@ -341,7 +341,7 @@ int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_si
     PHYLO_CHECK(build_carve(g, num_proteomes, (uint64_t)max_candidates, (void *)d_scratch,
                             (size_t)scratch_size, &a));
     cudaStream_t st = (cudaStream_t)stream;
-    PHYLO_CHECK(cudaMemcpyAsync(h_c1, a.c1 + (uint64_t)p * g.T1, sizeof(uint32_t) * g.T1,
+    PHYLO_CHECK(cudaMemcpyAsync(h_c1, a.c1 + (uint64_t)p * g.T1s, sizeof(uint32_t) * g.T1,
                                 cudaMemcpyDeviceToHost, st));
     PHYLO_CHECK(cudaMemcpyAsync(h_c2, a.c2 + (uint64_t)p * g.T2, sizeof(uint32_t) * g.T2,
                                 cudaMemcpyDeviceToHost, st));
@@ -435,6 +435,29 @@ int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int 
 
 long phyloSelfDotPartBytes(int num_vectors, long max_vector_len) {
     return (long)(self_dot_part_count((uint32_t)num_vectors, (uint64_t)max_vector_len) * sizeof(FF));
+}
+
+// Scratch bytes of phyloComparePairsMany for P pairs and at most max_tiles
+// merge tiles (sum over pairs of ceil((nl + nr) / 4096)).
+long phyloComparePairsManyScratch(int num_pairs, long max_tiles) {
+    return (long)compare_many_scratch_bytes((uint32_t)num_pairs, (uint64_t)max_tiles);
+}
+
+// C of many pairs in one merge-path launch sequence: pair p compares vector
+// pa[p] of the left arena with vector pb[p] of the right arena (arena =
+// keys, values, uint64 offsets, uint32 sizes); results to d_out[p] (double).
+// Asynchronous.
+int phyloComparePairsMany(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                          uintptr_t d_lkeys, uintptr_t d_lvalues, uintptr_t d_loff,
+                          uintptr_t d_lnnz, uintptr_t d_rkeys, uintptr_t d_rvalues,
+                          uintptr_t d_roff, uintptr_t d_rnnz, uintptr_t d_pa, uintptr_t d_pb,
+                          int num_pairs, long max_tiles, uintptr_t d_out) {
+    return (int)compare_many_launch(
+        (cudaStream_t)stream, (void *)d_scratch, (size_t)scratch_size, (const uint32_t *)d_lkeys,
+        (const float *)d_lvalues, (const uint64_t *)d_loff, (const uint32_t *)d_lnnz,
+        (const uint32_t *)d_rkeys, (const float *)d_rvalues, (const uint64_t *)d_roff,
+        (const uint32_t *)d_rnnz, (const uint32_t *)d_pa, (const uint32_t *)d_pb,
+        (uint32_t)num_pairs, (uint64_t)max_tiles, (double *)d_out, nullptr);
 }
 
 // Pair kernel launch on raw arena pointers for one pair, through the merge

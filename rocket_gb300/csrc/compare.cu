@@ -21,6 +21,7 @@
 // boundaries (never leaving the 16-byte block of a valid element) and the
 // consumer indexes from the offset.
 #include "compare.cuh"
+#include "scan.cuh"
 
 #include <mutex>
 
@@ -87,22 +88,15 @@ struct Stage {
     uint32_t nbx;  // nb plus one look-ahead right element when the right list continues
 };
 
-// Issues the bulk copies of tile `t` into buffer `buf`; returns the stage layout.
-__device__ __forceinline__ Stage issue_tile(uint32_t t, const uint32_t *splits, uint64_t total,
-                                            uint32_t nb_total, const uint32_t *Ak, const float *Av,
-                                            const uint32_t *Bk, const float *Bv, uint32_t *sk,
-                                            float *sv, uint64_t *bar, bool issue) {
+// Issues the bulk copies of left [i0, i1) and right [j0, j1x) (j1x = j1 or
+// j1 + 1 with the look-ahead element) into one stage buffer; returns the layout.
+__device__ __forceinline__ Stage issue_ranges(const uint32_t *Ak, const float *Av, uint32_t i0,
+                                              uint32_t i1, const uint32_t *Bk, const float *Bv,
+                                              uint32_t j0, uint32_t j1, uint32_t j1x, uint32_t *sk,
+                                              float *sv, uint64_t *bar, bool issue) {
     Stage s;
-    const uint64_t d0 = (uint64_t)t * CMP_TILE;
-    const uint64_t d1 = min(d0 + CMP_TILE, total);
-    const uint32_t i0 = splits[t], i1 = splits[t + 1];
-    const uint32_t j0 = (uint32_t)(d0 - i0), j1 = (uint32_t)(d1 - i1);
     s.na = i1 - i0;
     s.nb = j1 - j0;
-    // A match whose left element ends this tile can have its equal right element
-    // start the next one (ties go left), so one right element past the tile is
-    // copied as look-ahead.
-    const uint32_t j1x = j1 < nb_total ? j1 + 1 : j1;
     s.nbx = j1x - j0;
     // widened byte ranges
     const uintptr_t ka0 = (uintptr_t)(Ak + i0), ka1 = (uintptr_t)(Ak + i1);
@@ -128,6 +122,56 @@ __device__ __forceinline__ Stage issue_tile(uint32_t t, const uint32_t *splits, 
         if (bvb) bulk_g2s(sv + bva / 4, (const void *)lo16(vb0), bvb, bar);
     }
     return s;
+}
+
+// Issues the bulk copies of tile `t` of one pair into a stage buffer.
+__device__ __forceinline__ Stage issue_tile(uint32_t t, const uint32_t *splits, uint64_t total,
+                                            uint32_t nb_total, const uint32_t *Ak, const float *Av,
+                                            const uint32_t *Bk, const float *Bv, uint32_t *sk,
+                                            float *sv, uint64_t *bar, bool issue) {
+    const uint64_t d0 = (uint64_t)t * CMP_TILE;
+    const uint64_t d1 = min(d0 + CMP_TILE, total);
+    const uint32_t i0 = splits[t], i1 = splits[t + 1];
+    const uint32_t j0 = (uint32_t)(d0 - i0), j1 = (uint32_t)(d1 - i1);
+    // A match whose left element ends this tile can have its equal right element
+    // start the next one (ties go left), so one right element past the tile is
+    // copied as look-ahead.
+    const uint32_t j1x = j1 < nb_total ? j1 + 1 : j1;
+    return issue_ranges(Ak, Av, i0, i1, Bk, Bv, j0, j1, j1x, sk, sv, bar, issue);
+}
+
+// Per-thread merge path over 16 diagonals of a staged tile; adds the exact
+// products of matching keys to acc.
+__device__ __forceinline__ void merge_tile(const Stage &s, const uint32_t *skb, const float *svb,
+                                           FF &acc) {
+    const uint32_t *ka = skb + s.ka_off;
+    const float *va = svb + s.va_off;
+    const uint32_t *kb = skb + s.kb_off;
+    const float *vb = svb + s.vb_off;
+    const uint32_t d = threadIdx.x * CMP_IPT;
+    const uint32_t n = s.na + s.nb;
+    if (d >= n) return;
+    uint32_t lo = d > s.nb ? d - s.nb : 0u;
+    uint32_t hi = d < s.na ? d : s.na;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) / 2 + 1;
+        if (ka[mid - 1] <= kb[d - mid]) lo = mid; else hi = mid - 1;
+    }
+    uint32_t i = lo, j = d - lo;
+    const uint32_t steps = min((uint32_t)CMP_IPT, n - d);
+    for (uint32_t it = 0; it < steps; it++) {
+        const bool has_a = i < s.na, has_b = j < s.nb, has_bx = j < s.nbx;
+        const uint32_t x = has_a ? ka[i] : 0u, y = has_bx ? kb[j] : 0u;
+        const bool take_a = has_a && (!has_b || x <= y);
+        if (take_a && has_bx && x == y) {
+            float p, e;
+            two_prod(va[i], vb[j], p, e);
+            ff_add(acc, p);
+            acc.lo = __fadd_rn(acc.lo, e);
+        }
+        i += take_a;
+        j += !take_a;
+    }
 }
 
 __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
@@ -181,36 +225,7 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
         const Stage s = b ? stg1 : stg0;
         uint32_t *skb = b ? sk[1] : sk[0];
         float *svb = b ? sv[1] : sv[0];
-        const uint32_t *ka = skb + s.ka_off;
-        const float *va = svb + s.va_off;
-        const uint32_t *kb = skb + s.kb_off;
-        const float *vb = svb + s.vb_off;
-        // per-thread merge path inside the tile
-        const uint32_t d = threadIdx.x * CMP_IPT;
-        const uint32_t n = s.na + s.nb;
-        if (d < n) {
-            uint32_t lo = d > s.nb ? d - s.nb : 0u;
-            uint32_t hi = d < s.na ? d : s.na;
-            while (lo < hi) {
-                uint32_t mid = (lo + hi) / 2 + 1;
-                if (ka[mid - 1] <= kb[d - mid]) lo = mid; else hi = mid - 1;
-            }
-            uint32_t i = lo, j = d - lo;
-            const uint32_t steps = min((uint32_t)CMP_IPT, n - d);
-            for (uint32_t it = 0; it < steps; it++) {
-                const bool has_a = i < s.na, has_b = j < s.nb, has_bx = j < s.nbx;
-                const uint32_t x = has_a ? ka[i] : 0u, y = has_bx ? kb[j] : 0u;
-                const bool take_a = has_a && (!has_b || x <= y);
-                if (take_a && has_bx && x == y) {
-                    float p, e;
-                    two_prod(va[i], vb[j], p, e);
-                    ff_add(acc, p);
-                    acc.lo = __fadd_rn(acc.lo, e);
-                }
-                i += take_a;
-                j += !take_a;
-            }
-        }
+        merge_tile(s, skb, svb, acc);
         __syncthreads();  // everyone done with buffer b
         const uint32_t tn = t + 2;
         if (tn < t_end) {
@@ -388,6 +403,229 @@ cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const
     PHYLO_CHECK(static_scratch_address(&scratch));
     return compare_launch(stream, scratch, kStaticCompareBytes, lk, lv, nl, rk, rv, nr, d_out,
                           status_out);
+}
+
+// ---------------------------------------------------------------------------
+// Many pairs per launch.  Tiles of all pairs form one index space (pair p owns
+// tiles [tile_off[p], tile_off[p+1])), persistent CTAs walk contiguous runs of
+// it with the same double-buffered bulk copies, every tile leaves one
+// float-float partial, and k_many_reduce sums each pair's tiles in order.
+// ---------------------------------------------------------------------------
+
+struct ManyArgs {
+    const uint32_t *lkeys; const float *lvals; const uint64_t *loff; const uint32_t *lnnz;
+    const uint32_t *rkeys; const float *rvals; const uint64_t *roff; const uint32_t *rnnz;
+    const uint32_t *pa, *pb;   // pair p = (left vector pa[p], right vector pb[p])
+    uint32_t P;
+    uint32_t *ptiles;          // [P] tiles per pair
+    uint64_t *tile_off;        // [P+1]
+    uint64_t *scan_tmp;
+    uint32_t *splits;          // [T] left split at each tile start
+    FF *tile_part;             // [T]
+    uint64_t max_tiles;
+    double *out;               // [P]
+    uint32_t *status;
+};
+
+__device__ __forceinline__ uint32_t owner_of(const uint64_t *off, uint32_t n, uint64_t t) {
+    uint32_t lo = 0, hi = n;  // largest p with off[p] <= t
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= t) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_many_tiles(ManyArgs a) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const uint64_t tot = (uint64_t)a.lnnz[a.pa[p]] + a.rnnz[a.pb[p]];
+    a.ptiles[p] = (uint32_t)div_up(tot, CMP_TILE);
+}
+
+// one warp per tile start; grid-stride over the tiles
+__global__ void k_many_partition(ManyArgs a) {
+    const uint64_t T = a.tile_off[a.P];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = T > a.max_tiles ? DEV_CAPACITY : 0u;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+    for (uint64_t t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); t < T && t < a.max_tiles;
+         t += warps) {
+        const uint32_t p = owner_of(a.tile_off, a.P, t);
+        const uint32_t va = a.pa[p], vb = a.pb[p];
+        const uint32_t na = a.lnnz[va], nb = a.rnnz[vb];
+        const uint64_t d = (t - a.tile_off[p]) * CMP_TILE;
+        const uint32_t i = warp_merge_path(d, a.lkeys + a.loff[va], na, a.rkeys + a.roff[vb], nb);
+        if ((threadIdx.x & 31) == 0) a.splits[t] = i;
+    }
+}
+
+struct ManyTile {
+    uint32_t i0, i1, j0, j1, j1x;
+    uint32_t va, vb;
+};
+
+__device__ __forceinline__ ManyTile many_tile(const ManyArgs &a, uint64_t t) {
+    ManyTile m;
+    const uint32_t p = owner_of(a.tile_off, a.P, t);
+    m.va = a.pa[p];
+    m.vb = a.pb[p];
+    const uint32_t na = a.lnnz[m.va], nb = a.rnnz[m.vb];
+    const uint64_t total = (uint64_t)na + nb;
+    const uint64_t lt = t - a.tile_off[p];
+    const uint64_t d0 = lt * CMP_TILE, d1 = min(d0 + CMP_TILE, total);
+    m.i0 = a.splits[t];
+    m.i1 = (t + 1 < a.tile_off[p + 1]) ? a.splits[t + 1] : na;
+    m.j0 = (uint32_t)(d0 - m.i0);
+    m.j1 = (uint32_t)(d1 - m.i1);
+    m.j1x = m.j1 < nb ? m.j1 + 1 : m.j1;
+    return m;
+}
+
+__device__ __forceinline__ Stage many_issue(const ManyArgs &a, uint64_t t, uint32_t *sk, float *sv,
+                                            uint64_t *bar, bool issue) {
+    const ManyTile m = many_tile(a, t);
+    return issue_ranges(a.lkeys + a.loff[m.va], a.lvals + a.loff[m.va], m.i0, m.i1,
+                        a.rkeys + a.roff[m.vb], a.rvals + a.roff[m.vb], m.j0, m.j1, m.j1x, sk, sv,
+                        bar, issue);
+}
+
+__global__ void __launch_bounds__(CMP_THREADS) k_many_intersect(ManyArgs a) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    uint32_t *sk[2];
+    float *sv[2];
+    sk[0] = (uint32_t *)smem_raw;
+    sv[0] = (float *)(sk[0] + CMP_BUF);
+    sk[1] = (uint32_t *)(sv[0] + CMP_BUF);
+    sv[1] = (float *)(sk[1] + CMP_BUF);
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ FF warp_part[CMP_THREADS / 32];
+    __shared__ bool s_fail;
+    uint64_t T = a.tile_off[a.P];
+    if (T > a.max_tiles) T = a.max_tiles;
+    const uint64_t per = (T + gridDim.x - 1) / gridDim.x;
+    const uint64_t t_begin = (uint64_t)blockIdx.x * per;
+    const uint64_t t_end = min(T, t_begin + per);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        s_fail = false;
+    }
+    __syncthreads();
+    Stage stg0 = {0, 0, 0, 0, 0, 0, 0}, stg1 = {0, 0, 0, 0, 0, 0, 0};
+    if (t_begin < t_end) stg0 = many_issue(a, t_begin, sk[0], sv[0], &bar[0], threadIdx.x == 0);
+    if (t_begin + 1 < t_end) stg1 = many_issue(a, t_begin + 1, sk[1], sv[1], &bar[1], threadIdx.x == 0);
+    uint64_t fail_at = ~0ull;
+    for (uint64_t t = t_begin; t < t_end; t++) {
+        const int b = (int)((t - t_begin) & 1);
+        const uint32_t phase = (uint32_t)(((t - t_begin) >> 1) & 1);
+        if (!mbar_wait_bounded(&bar[b], phase)) s_fail = true;
+        __syncthreads();
+        if (s_fail) {
+            fail_at = t;
+            break;
+        }
+        FF acc = {0.0f, 0.0f};
+        merge_tile(b ? stg1 : stg0, b ? sk[1] : sk[0], b ? sv[1] : sv[0], acc);
+        acc = ff_warp_sum(acc);
+        if ((threadIdx.x & 31) == 0) warp_part[threadIdx.x >> 5] = acc;
+        __syncthreads();  // buffer b consumed, warp partials written
+        if (threadIdx.x == 0) {
+            FF r = {0.0f, 0.0f};
+            for (int w = 0; w < CMP_THREADS / 32; w++) r = ff_merge(r, warp_part[w]);
+            a.tile_part[t] = r;
+        }
+        const uint64_t tn = t + 2;
+        if (tn < t_end) {
+            if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const Stage ns = many_issue(a, tn, b ? sk[1] : sk[0], b ? sv[1] : sv[0], &bar[b],
+                                        threadIdx.x == 0);
+            if (b) stg1 = ns; else stg0 = ns;
+        }
+        __syncthreads();  // warp_part reused next tile
+    }
+    if (fail_at != ~0ull) {
+        if (threadIdx.x == 0) atomicOr(a.status, (uint32_t)DEV_WAIT_TIMEOUT);
+        for (uint64_t t = fail_at; t < t_end && t < fail_at + 2; t++) {
+            const uint64_t rel = t - t_begin;
+            (void)mbar_wait_bounded(&bar[rel & 1], (uint32_t)((rel >> 1) & 1), 1u << 16);
+        }
+    }
+}
+
+// one warp per pair: its tiles' partials in tile order (each lane a fixed
+// strided subset, then a fixed shuffle tree), double-double
+__global__ void k_many_reduce(ManyArgs a) {
+    const uint32_t p = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (p >= a.P) return;
+    const int lane = threadIdx.x & 31;
+    const uint64_t t0 = a.tile_off[p], t1 = a.tile_off[p + 1];
+    DD acc = {0.0, 0.0};
+    for (uint64_t t = t0 + lane; t < t1 && t < a.max_tiles; t += 32) {
+        dd_add(acc, (double)a.tile_part[t].hi);
+        dd_add(acc, (double)a.tile_part[t].lo);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        DD o;
+        o.hi = __shfl_down_sync(0xffffffffu, acc.hi, d);
+        o.lo = __shfl_down_sync(0xffffffffu, acc.lo, d);
+        acc = dd_merge(acc, o);
+    }
+    if (lane == 0) a.out[p] = __dadd_rn(acc.hi, acc.lo);
+}
+
+size_t compare_many_scratch_bytes(uint32_t P, uint64_t max_tiles) {
+    return scratch_bytes<uint32_t>(P) + scratch_bytes<uint64_t>((uint64_t)P + 1) +
+           scan_temp_bytes((uint64_t)P + 1) + scratch_bytes<uint32_t>(max_tiles) +
+           scratch_bytes<FF>(max_tiles) + scratch_bytes<uint32_t>(4);
+}
+
+cudaError_t compare_many_launch(cudaStream_t st, void *scratch, size_t scratch_size,
+                                const uint32_t *lkeys, const float *lvals, const uint64_t *loff,
+                                const uint32_t *lnnz, const uint32_t *rkeys, const float *rvals,
+                                const uint64_t *roff, const uint32_t *rnnz, const uint32_t *pa,
+                                const uint32_t *pb, uint32_t P, uint64_t max_tiles, double *out,
+                                uint32_t **status_out) {
+    if (P == 0) return cudaSuccess;
+    Scratch sc(scratch, scratch_size);
+    ManyArgs a;
+    a.lkeys = lkeys; a.lvals = lvals; a.loff = loff; a.lnnz = lnnz;
+    a.rkeys = rkeys; a.rvals = rvals; a.roff = roff; a.rnnz = rnnz;
+    a.pa = pa; a.pb = pb; a.P = P;
+    a.ptiles = sc.take<uint32_t>(P);
+    a.tile_off = sc.take<uint64_t>((uint64_t)P + 1);
+    a.scan_tmp = sc.take<uint64_t>(scan_temp_bytes((uint64_t)P + 1) / 8);
+    a.splits = sc.take<uint32_t>(max_tiles);
+    a.tile_part = sc.take<FF>(max_tiles);
+    a.status = sc.take<uint32_t>(4);
+    a.max_tiles = max_tiles;
+    a.out = out;
+    if (!a.status) return cudaErrorInvalidValue;
+    if (status_out) *status_out = a.status;
+    {
+        static uint64_t attr_done = 0;
+        int dev = 0;
+        PHYLO_CHECK(cudaGetDevice(&dev));
+        if (dev < 64 && !(attr_done >> dev & 1)) {
+            PHYLO_CHECK(cudaFuncSetAttribute(
+                k_many_intersect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCmpSmem));
+            attr_done |= 1ull << dev;
+        }
+    }
+    k_many_tiles<<<(P + 255) / 256, 256, 0, st>>>(a);
+    PHYLO_CHECK(scan_u32_to_u64(a.ptiles, P, a.tile_off, a.scan_tmp, st));
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    k_many_partition<<<sms * 4, 256, 0, st>>>(a);
+    k_many_intersect<<<sms * 3, CMP_THREADS, kCmpSmem, st>>>(a);
+    k_many_reduce<<<(P + 7) / 8, 256, 0, st>>>(a);
+    return cudaGetLastError();
 }
 
 }  // namespace phylo

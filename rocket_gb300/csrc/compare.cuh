@@ -22,4 +22,14 @@ cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const
 uint64_t compare_static_max_entries();
 size_t compare_static_bytes();
 
+// Many pairs per launch: C of pair p = (left vector pa[p], right vector pb[p])
+// to out[p].  max_tiles bounds sum over pairs of ceil((nl + nr) / 4096).
+size_t compare_many_scratch_bytes(uint32_t P, uint64_t max_tiles);
+cudaError_t compare_many_launch(cudaStream_t st, void *scratch, size_t scratch_size,
+                                const uint32_t *lkeys, const float *lvals, const uint64_t *loff,
+                                const uint32_t *lnnz, const uint32_t *rkeys, const float *rvals,
+                                const uint64_t *roff, const uint32_t *rnnz, const uint32_t *pa,
+                                const uint32_t *pb, uint32_t P, uint64_t max_tiles, double *out,
+                                uint32_t **status_out);
+
 }  // namespace phylo

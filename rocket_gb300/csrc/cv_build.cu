@@ -214,6 +214,45 @@ __global__ void k_prep(int B, const uint64_t *__restrict__ seq_off, uint64_t *ti
     }
 }
 
+// Alpha of every small count tuple, once per proteome (the same arithmetic as
+// markov_alpha_fast, so a table hit gives the bits the direct path would).
+// grid = (TUPLE_TABLE / 256, B)
+__global__ void k_tuple_alpha(BuildArgs a) {
+    const int p = blockIdx.y;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint32_t)TUPLE_TABLE) return;
+    const uint32_t mid = t % TUPLE_MID, suf = (t / TUPLE_MID) % TUPLE_PS,
+                   pre = (t / (TUPLE_MID * TUPLE_PS)) % TUPLE_PS,
+                   full = t / (TUPLE_MID * TUPLE_PS * TUPLE_PS);
+    const uint32_t n0 = a.tot[p * 4 + 0], n1 = a.tot[p * 4 + 1], n2 = a.tot[p * 4 + 2];
+    uint32_t bits = 0;
+    if (full >= 1 && pre >= 1 && suf >= 1 && mid >= 1 && n0 != 0)
+        bits = __float_as_uint(markov_alpha_fast(full, pre, suf, mid, n0, n1, n2,
+                                                 a.prob + (uint64_t)p * 4 * PROB_TABLE));
+    a.atab[(uint64_t)p * TUPLE_TABLE + t] = bits;
+}
+
+__device__ __forceinline__ float div_by_scale(float f, double scale, double rs) {
+    const double x = (double)f;
+    const double q = __dmul_rn(x, rs);
+    return __double2float_rn(__fma_rn(__fma_rn(-q, scale, x), rs, q));
+}
+
+// Normalised value of every tuple, after the norm is known.  grid = (TUPLE_TABLE / 256, B)
+__global__ void k_tuple_value(BuildArgs a) {
+    const int p = blockIdx.y;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint32_t)TUPLE_TABLE) return;
+    const double scale = a.scale[p], rs = a.rscale[p];
+    const float f = __uint_as_float(a.atab[(uint64_t)p * TUPLE_TABLE + t]);
+    float v;
+    if (!(isfinite(scale) && scale > 0.0) || !isfinite(f))
+        v = __double2float_rn(__ddiv_rn((double)f, scale));
+    else
+        v = div_by_scale(f, scale, rs);
+    a.vtab[(uint64_t)p * TUPLE_TABLE + t] = v;
+}
+
 // Counts (K-2)- and (K-1)-windows, marks right extensions, totals n0/n1/n2.
 // A window starting at i counts for length L when its L symbols are all in the
 // alphabet and inside the proteome (native.cu:236-252).
@@ -233,7 +272,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             dig[j] = pos < len ? (uint8_t)char_to_digit(a.alpha, a.seq[s0 + pos]) : (uint8_t)0xff;
         }
         __syncthreads();
-        uint32_t *c1 = a.c1 + (uint64_t)p * a.T1;
+        uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
         uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
         uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         uint32_t cnt0 = 0, cnt1 = 0, cnt2 = 0;
@@ -283,19 +322,34 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
     }
 }
 
-__device__ __forceinline__ uint32_t cand_count_of(const BuildArgs &a, int p, uint64_t q) {
-    if (q >= a.T1) return 0;
-    uint32_t c = a.c1[(uint64_t)p * a.T1 + q];
-    if (!c) return 0;
-    return __popc(a.mask[(uint64_t)p * a.T2 + a.fdT2.mod((uint32_t)q)]);
+// Candidate counts of the 8 consecutive (K-1)-mers q0..q0+7 (q0 a multiple of 8).
+// Rows of the (K-1)-mer tables are padded to T1s (a multiple of 8) with zero
+// counts, so 16-byte accesses stay aligned and in the row.
+__device__ __forceinline__ void cand_counts8(const BuildArgs &a, int p, uint32_t q0,
+                                             uint32_t (&v)[8]) {
+    const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
+    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const uint32_t qb = q0 + 4 * h;
+        uint4 c = make_uint4(0, 0, 0, 0);
+        if (qb < a.T1) c = __ldg(reinterpret_cast<const uint4 *>(c1 + qb));
+        const uint32_t cs[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            v[4 * h + u] = cs[u] ? __popc(__ldg(&mk[a.fdT2.mod(qb + u)])) : 0u;
+    }
 }
 
 // Candidates per chunk of CH (K-1)-mers.  grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     const int p = blockIdx.y, c = blockIdx.x;
-    const uint64_t q0 = (uint64_t)c * CH;
+    const uint32_t q0 = (uint32_t)c * CH + threadIdx.x * (CH / CHUNK_THREADS);
+    uint32_t v[8];
+    cand_counts8(a, p, q0, v);
     uint32_t s = 0;
-    for (int i = threadIdx.x; i < CH; i += CHUNK_THREADS) s += cand_count_of(a, p, q0 + i);
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += v[i];
     s = __reduce_add_sync(0xffffffffu, s);
     __shared__ uint32_t ws[CHUNK_THREADS / 32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -312,25 +366,26 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
     const int p = blockIdx.y, c = blockIdx.x;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
-    const uint64_t q0 = (uint64_t)c * CH;
-    constexpr int PER = CH / CHUNK_THREADS;
-    uint32_t v[PER];
+    const uint32_t q0 = (uint32_t)c * CH + threadIdx.x * (CH / CHUNK_THREADS);
+    uint32_t v[8];
+    cand_counts8(a, p, q0, v);
     uint64_t s = 0;
 #pragma unroll
-    for (int i = 0; i < PER; i++) {
-        v[i] = cand_count_of(a, p, q0 + threadIdx.x * PER + i);
-        s += v[i];
-    }
+    for (int i = 0; i < 8; i++) s += v[i];
     uint64_t tot;
     uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
-    uint64_t base = a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH];
-    uint32_t *coff = a.coff + (uint64_t)p * a.T1;
+    const uint32_t base =
+        (uint32_t)(a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH] + ex);
+    uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
+    uint32_t o[8];
+    uint32_t run = base;
 #pragma unroll
-    for (int i = 0; i < PER; i++) {
-        uint64_t q = q0 + threadIdx.x * PER + i;
-        if (q < a.T1) coff[q] = (uint32_t)(base + ex);
-        ex += v[i];
+    for (int i = 0; i < 8; i++) {
+        o[i] = run;
+        run += v[i];
     }
+    if (q0 < a.T1) *reinterpret_cast<uint4 *>(coff + q0) = make_uint4(o[0], o[1], o[2], o[3]);
+    if (q0 + 4 < a.T1) *reinterpret_cast<uint4 *>(coff + q0 + 4) = make_uint4(o[4], o[5], o[6], o[7]);
 }
 
 // zero the K-mer count slots of all candidates (bounded by capacity)
@@ -360,7 +415,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
             dig[j] = pos < len ? (uint8_t)char_to_digit(a.alpha, a.seq[s0 + pos]) : (uint8_t)0xff;
         }
         __syncthreads();
-        const uint32_t *coff = a.coff + (uint64_t)p * a.T1;
+        const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
         const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         const uint64_t cbase = a.chunk_cand_off[(uint64_t)p * a.NCH];
         for (int u = 0; u < TILE / COUNT_THREADS; u++) {
@@ -427,11 +482,12 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     const uint32_t ncand = (uint32_t)(a.chunk_cand_off[pc + 1] - cb);
     const uint64_t q0 = (uint64_t)c * CH;
     const uint32_t nq = (uint32_t)min((uint64_t)CH, a.T1 - q0);
-    const uint32_t *coff = a.coff + (uint64_t)p * a.T1;
-    const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1;
+    const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
+    const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
     const uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
     const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
     const double *prob = a.prob + (uint64_t)p * 4 * PROB_TABLE;
+    const uint32_t *atab = a.atab + (uint64_t)p * TUPLE_TABLE;
     const uint32_t n0 = a.tot[p * 4 + 0], n1 = a.tot[p * 4 + 1], n2 = a.tot[p * 4 + 2];
     uint32_t local0 = ncand ? coff[q0] : 0;
     for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
@@ -450,9 +506,20 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
         const uint32_t pre = c1[q];
         const uint32_t suf = c1[m * A + b];
         const uint32_t mid = c2[m];
-        const float f = markov_alpha_fast(full, pre, suf, mid, n0, n1, n2, prob);
+        float f;
+        uint32_t stored;
+        if (full - 1u < 3u && pre < (uint32_t)TUPLE_PS && suf < (uint32_t)TUPLE_PS &&
+            mid < (uint32_t)TUPLE_MID && n0 != 0u) {
+            const uint32_t t = ((full * TUPLE_PS + pre) * TUPLE_PS + suf) * TUPLE_MID + mid;
+            const uint32_t tb = __ldg(&atab[t]);
+            f = __uint_as_float(tb);
+            stored = tb ? (TUPLE_TAG | t) : 0u;
+        } else {
+            f = markov_alpha_fast(full, pre, suf, mid, n0, n1, n2, prob);
+            stored = __float_as_uint(f);
+        }
         const uint32_t bits = __float_as_uint(f);
-        a.c0a[cb + u] = bits;
+        a.c0a[cb + u] = stored;
         if (bits != 0u) {
             surv++;
             const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
@@ -546,13 +613,14 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
     if (a.chunk_surv[pc] == 0) return;
     const uint64_t q0 = (uint64_t)c * CH;
     const uint32_t nq = (uint32_t)min((uint64_t)CH, a.T1 - q0);
-    const uint32_t *coff = a.coff + (uint64_t)p * a.T1;
+    const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
     const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
     uint32_t local0 = coff[q0];
     for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
     __syncthreads();
     const double scale = a.scale[p];
     const double rs = a.rscale[p];
+    const float *vtab = a.vtab + (uint64_t)p * TUPLE_TABLE;
     const bool finite = isfinite(scale) && scale > 0.0;
     const float vm1 = __double2float_rn(-rs);  // RN(-1/scale) == -RN(1/scale)
     // destination: proteome base in the caller's arena + offset within proteome
@@ -581,14 +649,14 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
             if (o < dst_end) {
                 const float f = __uint_as_float(bits);
                 float v;
-                if (!finite || !isfinite(f)) {
+                if ((bits & TUPLE_TAG) == TUPLE_TAG) {
+                    v = __ldg(&vtab[bits & ~TUPLE_TAG]);
+                } else if (!finite || !isfinite(f)) {
                     v = __double2float_rn(__ddiv_rn((double)f, scale));
                 } else if (f == -1.0f) {
                     v = vm1;
                 } else {
-                    const double x = (double)f;
-                    const double q = __dmul_rn(x, rs);
-                    v = __double2float_rn(__fma_rn(__fma_rn(-q, scale, x), rs, q));
+                    v = div_by_scale(f, scale, rs);
                 }
                 a.out_keys[o] = key;
                 a.out_vals[o] = v;
@@ -611,6 +679,7 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     g->k = k;
     g->A = (uint32_t)A;
     g->T1 = ipow64(A, k - 1);
+    g->T1s = (g->T1 + 7) / 8 * 8;
     g->T2 = ipow64(A, k - 2);
     g->NCH = div_up(g->T1, CH);
     return 0;
@@ -619,8 +688,8 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
 size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     const uint64_t nc = (uint64_t)B * g.NCH;
     size_t s = 0;
-    s += scratch_bytes<uint32_t>(g.T1 * B);        // c1
-    s += scratch_bytes<uint32_t>(g.T1 * B);        // coff
+    s += scratch_bytes<uint32_t>(g.T1s * B);       // c1 (rows padded to 8 entries)
+    s += scratch_bytes<uint32_t>(g.T1s * B);       // coff
     s += scratch_bytes<uint32_t>(g.T2 * B);        // c2
     s += scratch_bytes<uint32_t>(g.T2 * B);        // mask
     s += scratch_bytes<uint32_t>(4 * (uint64_t)B); // tot
@@ -634,6 +703,8 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     s += scratch_bytes<uint64_t>(3 * nc);          // chunk_norm
     s += scratch_bytes<uint32_t>(nc);              // chunk_bad
     s += scratch_bytes<double>(4 * (uint64_t)PROB_TABLE * B);  // prob tables
+    s += scratch_bytes<uint32_t>((uint64_t)TUPLE_TABLE * B);   // atab
+    s += scratch_bytes<float>((uint64_t)TUPLE_TABLE * B);      // vtab
     s += scratch_bytes<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);  // scan temp
     s += scratch_bytes<double>(B);                 // norm
     s += scratch_bytes<double>(B);                 // scale
@@ -653,8 +724,9 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     const uint64_t nc = (uint64_t)B * g.NCH;
     BuildArgs &r = *a;
     r.alpha = g.alpha; r.k = g.k; r.A = g.A; r.T1 = g.T1; r.T2 = g.T2; r.NCH = g.NCH; r.B = B;
-    r.c1 = sc.take<uint32_t>(g.T1 * B);
-    r.coff = sc.take<uint32_t>(g.T1 * B);
+    r.T1s = g.T1s;
+    r.c1 = sc.take<uint32_t>(g.T1s * B);
+    r.coff = sc.take<uint32_t>(g.T1s * B);
     r.c2 = sc.take<uint32_t>(g.T2 * B);
     r.mask = sc.take<uint32_t>(g.T2 * B);
     r.tot = sc.take<uint32_t>(4 * (uint64_t)B);
@@ -668,6 +740,8 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.chunk_norm = sc.take<uint64_t>(3 * nc);
     r.chunk_bad = sc.take<uint32_t>(nc);
     r.prob = sc.take<double>(4 * (uint64_t)PROB_TABLE * B);
+    r.atab = sc.take<uint32_t>((uint64_t)TUPLE_TABLE * B);
+    r.vtab = sc.take<float>((uint64_t)TUPLE_TABLE * B);
     r.fdT2.set((uint32_t)g.T2);
     r.scan_tmp = sc.take<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);
     r.norm = sc.take<double>(B);
@@ -699,7 +773,7 @@ static int sm_count() {
 cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const uint64_t nc = (uint64_t)a.B * a.NCH;
     // dense tables c1 | coff | c2 | mask | tot are contiguous in scratch: zero what needs it
-    PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1 * a.B, st));
+    PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1s * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.mask, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.tot, 0, sizeof(uint32_t) * 4 * a.B, st));
@@ -708,6 +782,7 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const int grid_seq = sm_count() * 8;
     k_count<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
     k_tables<<<dim3(PROB_TABLE / 256, a.B), 256, 0, st>>>(a);
+    k_tuple_alpha<<<dim3(TUPLE_TABLE / 256, a.B), 256, 0, st>>>(a);
     dim3 gch((unsigned)a.NCH, (unsigned)a.B);
     k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
@@ -717,6 +792,7 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     k_alpha<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_surv, nc, a.chunk_out_off, a.scan_tmp, st));
     k_norm<<<a.B, 32, 0, st>>>(a);
+    k_tuple_value<<<dim3(TUPLE_TABLE / 256, a.B), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -729,9 +805,9 @@ cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
 
 // Kernel counting per launch of build_plan + build_emit (for launch accounting).
 // Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_tables,
-// k_cand_count, scan (3), k_cand_offsets, k_c0_zero, k_c0_scatter, k_alpha,
-// scan (3), k_norm; emit k_arena_offsets, k_compact, k_arena_pad.  (Five
-// memsets are not counted.)
-int build_launches_per_batch() { return 15 + 3; }
+// k_tuple_alpha, k_cand_count, scan (3), k_cand_offsets, k_c0_zero,
+// k_c0_scatter, k_alpha, scan (3), k_norm, k_tuple_value; emit
+// k_arena_offsets, k_compact, k_arena_pad.  (Five memsets are not counted.)
+int build_launches_per_batch() { return 17 + 3; }
 
 }  // namespace phylo

@@ -8,6 +8,7 @@ struct BuildGeometry {
     int alpha, k;
     uint32_t A;      // alphabet size (21 protein, 4 DNA)
     uint64_t T1, T2; // A^(K-1), A^(K-2)
+    uint64_t T1s;    // per-proteome row length of the (K-1)-mer tables (T1 rounded up to 8)
     uint64_t NCH;    // chunks of (K-1)-mers per proteome
 };
 
@@ -27,11 +28,20 @@ struct FastDiv {
 // Count -> probability tables are kept for counts below this bound.
 constexpr int PROB_TABLE = 4096;
 
+// Alpha / value tables over small count tuples (full, prefix, suffix, middle):
+// full in 1..3 (2 bits), prefix and suffix below 8 (3 bits each), middle below
+// 128 (7 bits); index = ((full*8 + prefix)*8 + suffix)*128 + middle.
+constexpr int TUPLE_FULL = 4, TUPLE_PS = 8, TUPLE_MID = 128;
+constexpr int TUPLE_TABLE = TUPLE_FULL * TUPLE_PS * TUPLE_PS * TUPLE_MID;  // 32768
+// A candidate whose alpha came from the tuple table keeps TUPLE_TAG | index in
+// place of its alpha bits (a negative-NaN pattern no computed alpha produces).
+constexpr uint32_t TUPLE_TAG = 0xffff0000u;
+
 // Everything a build launch needs; plain device pointers, passed by value.
 struct BuildArgs {
     int alpha, k, B;
     uint32_t A;
-    uint64_t T1, T2, NCH;
+    uint64_t T1, T2, T1s, NCH;
     // input: concatenated sequences, seq_off[B+1] (device)
     const uint8_t *seq;
     const uint64_t *seq_off;
@@ -50,6 +60,8 @@ struct BuildArgs {
     uint64_t *chunk_norm;     // [nc][3]: sum of the other alpha^2 as 192-bit fixed point, 2^-96 units
     uint32_t *chunk_bad;      // [nc]: bit 0 a NaN square, bit 1 an infinite one
     double *prob;             // [B][4][PROB_TABLE]: c/n0, c/n1, c/n2, 1/(c/n2)
+    uint32_t *atab;           // [B][TUPLE_TABLE]: alpha bits of each count tuple
+    float *vtab;              // [B][TUPLE_TABLE]: float(alpha / sqrt(norm)) of each tuple
     FastDiv fdT2;             // division by A^(K-2)
     uint64_t *scan_tmp;
     // per proteome results

@@ -42,7 +42,7 @@ __device__ __forceinline__ uint64_t block_excl_scan_u64(uint64_t v, uint64_t *sm
     return r;
 }
 
-__global__ void k_scan_reduce(const uint32_t *__restrict__ in, uint64_t n, uint64_t *partials) {
+static __global__ void k_scan_reduce(const uint32_t *__restrict__ in, uint64_t n, uint64_t *partials) {
     __shared__ uint64_t sw[SCAN_THREADS / 32 + 1];
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
     uint64_t s = 0;
@@ -57,7 +57,7 @@ __global__ void k_scan_reduce(const uint32_t *__restrict__ in, uint64_t n, uint6
 }
 
 // Single CTA: exclusive scan of the partials in place; total to partials[np].
-__global__ void k_scan_partials(uint64_t *partials, uint64_t np) {
+static __global__ void k_scan_partials(uint64_t *partials, uint64_t np) {
     __shared__ uint64_t sw[SCAN_THREADS / 32 + 1];
     uint64_t carry = 0;
     for (uint64_t base = 0; base < np; base += SCAN_THREADS) {
@@ -72,7 +72,7 @@ __global__ void k_scan_partials(uint64_t *partials, uint64_t np) {
 }
 
 // Writes out[i] = exclusive prefix; out[n] = total.
-__global__ void k_scan_apply(const uint32_t *__restrict__ in, uint64_t n,
+static __global__ void k_scan_apply(const uint32_t *__restrict__ in, uint64_t n,
                              const uint64_t *__restrict__ partials, uint64_t *out) {
     __shared__ uint64_t sw[SCAN_THREADS / 32 + 1];
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;

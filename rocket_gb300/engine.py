@@ -434,6 +434,165 @@ class PairEngine:
                         flat[c * plan.ldc + r] = flat[r * plan.ldc + c]
 
 
+    # -- merge-path algorithm over explicit pairs -------------------------------
+    def _nnz_dev(self, arena: Arena) -> torch.Tensor:
+        key = id(arena), arena.n
+        cache = getattr(self, "_nnz_cache", {})
+        if key not in cache:
+            cache[key] = torch.from_numpy(arena.nnz[:arena.n].astype(np.int32)).to(self.device)
+            self._nnz_cache = cache
+        return cache[key]
+
+    def compare_pairs_merge(self, pa, pb, col_arena: Optional[Arena] = None, stream=None,
+                            out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """C of pairs (pa[p] in this arena, pb[p] in col_arena) with the
+        multi-pair merge-path kernels; returns a float64 device tensor."""
+        a = self.arena
+        ca = col_arena if col_arena is not None else a
+        pa = np.asarray(pa, np.int64)
+        pb = np.asarray(pb, np.int64)
+        P = len(pa)
+        if out is None:
+            out = torch.empty(P, dtype=torch.float64, device=self.device)
+        if P == 0:
+            return out
+        tiles = int(np.sum((a.nnz[pa] + ca.nnz[pb] + 4095) // 4096))
+        nbytes = int(self.L.phyloComparePairsManyScratch(P, tiles))
+        if getattr(self, "_many_scratch", None) is None or self._many_scratch.numel() < nbytes:
+            self._many_scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        s_obj = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(s_obj):
+            dpa = torch.from_numpy(pa.astype(np.int32)).to(self.device, non_blocking=True)
+            dpb = torch.from_numpy(pb.astype(np.int32)).to(self.device, non_blocking=True)
+        check(self.L.phyloComparePairsMany(
+            int(s_obj.cuda_stream), _p(self._many_scratch), self._many_scratch.numel(),
+            _p(a.keys), _p(a.values), _p(a.vec_off), _p(self._nnz_dev(a)),
+            _p(ca.keys), _p(ca.values), _p(ca.vec_off), _p(self._nnz_dev(ca)),
+            _p(dpa), _p(dpb), P, tiles, _p(out)))
+        self.launches += 7
+        return out
+
+
+    # -- CUDA graph of the pair phase -----------------------------------------
+    def capture(self, plan: PairPlan, out: torch.Tensor, diagonal: bool = True,
+                col_arena: Optional[Arena] = None) -> torch.cuda.CUDAGraph:
+        """Captures counter reset, pair kernel, reduction (and self products)
+        for this plan into a CUDA graph; replay() reruns them with one launch.
+        The arena and plan buffers must stay alive and unchanged in shape."""
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        # warm run outside the capture: sizes scratch buffers, sets attributes
+        self.run(plan, out, stream=s, diagonal=diagonal, col_arena=col_arena)
+        s.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            self.run(plan, out, stream=s, diagonal=diagonal, col_arena=col_arena)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        return g
+
+
+# ------------------------------------------------------------------------------
+# autotuner
+# ------------------------------------------------------------------------------
+
+def _tune_cache_path() -> str:
+    import os
+    return os.environ.get("ROCKET_GB300_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "rocket_gb300",
+                                       "tune.json"))
+
+
+def tune_key(arena: Arena, n_rows: int, n_cols: int) -> str:
+    nnz = arena.nnz[:arena.n]
+    bucket = int(np.round(np.log2(max(float(nnz.mean()), 1.0)) * 2))
+    return f"{arena.alphabet}-k{arena.k}-r{int(np.log2(max(n_rows, 1)))}-c{int(np.log2(max(n_cols, 1)))}-n{bucket}"
+
+
+TUNE_SPACE = [
+    dict(wshift=10, fold=16, items_per_cta=4),
+    dict(wshift=10, fold=16, items_per_cta=2),
+    dict(wshift=10, fold=16, items_per_cta=8),
+    dict(wshift=9, fold=16, items_per_cta=4),
+    dict(wshift=11, fold=16, items_per_cta=4),
+    dict(wshift=10, fold=8, items_per_cta=4),
+]
+
+
+def autotune(arena: Arena, ids=None, space=None, repeats: int = 2, use_cache: bool = True,
+             include_merge: bool = True, verbose: bool = False) -> dict:
+    """Times the window kernel under each configuration of ``space`` (and the
+    merge-path kernel) on the all-pair plan of ``ids`` and returns the fastest,
+    caching it per (alphabet, K, size class) in a JSON file."""
+    import json
+    import os
+    import time
+    space = space or TUNE_SPACE
+    n = arena.n if ids is None else len(ids)
+    key = tune_key(arena, n, n)
+    path = _tune_cache_path()
+    cache = {}
+    if use_cache and os.path.exists(path):
+        try:
+            with open(path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+        if key in cache:
+            return cache[key]
+    results = []
+    out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device=arena.keys.device)
+    for cfg in space:
+        eng = PairEngine(arena, EngineConfig(**cfg))
+        saved = (arena.roff, arena.wshift, arena.R, arena.indexed)
+        if arena.wshift != cfg["wshift"]:
+            arena.roff, arena.indexed = None, 0
+        eng.ensure_index()
+        plan = eng.plan_triangle(ids)
+        eng.run(plan, out, diagonal=False)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(repeats):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            eng.run(plan, out, diagonal=False)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        results.append(dict(cfg, algorithm="window", ms=best))
+        if arena.wshift != saved[1]:
+            arena.roff, arena.wshift, arena.R, arena.indexed = saved
+        if verbose:
+            print(results[-1], flush=True)
+    if include_merge:
+        eng = PairEngine(arena)
+        idx = np.arange(arena.n) if ids is None else np.asarray(ids)
+        iu = np.triu_indices(len(idx), 1)
+        pa, pb = idx[iu[0]], idx[iu[1]]
+        eng.compare_pairs_merge(pa, pb)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            eng.compare_pairs_merge(pa, pb)
+            torch.cuda.synchronize()
+            best = min(best, 1000 * (time.perf_counter() - t0))
+        results.append(dict(algorithm="merge", ms=best))
+        if verbose:
+            print(results[-1], flush=True)
+    winner = min(results, key=lambda r: r["ms"])
+    entry = dict(winner, candidates=results)
+    if use_cache:
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            cache[key] = entry
+            with open(path, "w") as f:
+                json.dump(cache, f, indent=1)
+        except OSError:
+            pass
+    return entry
+
+
 def distances(c: torch.Tensor) -> torch.Tensor:
     """D = (1 - C) / 2."""
     return (1.0 - c) * 0.5

@@ -69,4 +69,4 @@ def test_batch_scratch_rejects_bad_arguments(lib):
     assert f("dna", 6, 4, 1000) == -1
     assert f("DNA", 10, 4, 1000) > 0
     assert lib.phyloBuildLaunchesPerBatch() > 0
-    assert lib.phyloPairsSmemBytes(10) == (1024 + 1) * 16 * 4 + 4 * 256 * 32  # table + ring
+    assert lib.phyloPairsSmemBytes(10) == (1024 + 1) * 80 + 2 * 256 * 32  # table + ring

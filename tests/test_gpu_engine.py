@@ -68,3 +68,37 @@ def test_window_index(small):
         keys, _ = arena.host_vector(v)
         expect = np.searchsorted(keys, np.arange(arena.R + 1, dtype=np.int64) << 10)
         assert np.array_equal(roff[v, :arena.R + 1], expect)
+
+
+def test_multi_pair_merge_matches_fp64(small):
+    p, arena, C_ref = small
+    eng = PairEngine(arena)
+    iu = np.triu_indices(arena.n, 1)
+    out = eng.compare_pairs_merge(iu[0], iu[1]).cpu().numpy()
+    err = np.abs(out - C_ref[iu]) / 2
+    assert err.max() <= 1e-9  # exact products, float-float sums
+
+
+def test_graph_replay_equals_eager(small):
+    p, arena, _ = small
+    eng = PairEngine(arena)
+    eng.ensure_index()
+    plan = eng.plan_triangle()
+    eager = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+    eng.run(plan, eager)
+    out = torch.zeros_like(eager)
+    g = eng.capture(plan, out)
+    out.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, eager)
+
+
+def test_autotune(small, tmp_path, monkeypatch):
+    from rocket_gb300.engine import autotune
+    p, arena, _ = small
+    monkeypatch.setenv("ROCKET_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    r = autotune(arena, repeats=1)
+    assert r["algorithm"] in ("window", "merge") and r["ms"] > 0
+    assert len(r["candidates"]) >= 2
+    assert autotune(arena)["ms"] == r["ms"]  # served from the cache
