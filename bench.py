@@ -37,9 +37,25 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = "uniform256"
-WORKLOAD_TEXT = ("uniform256: 256 synthetic proteomes x 1,500 proteins (lognormal lengths, "
-                 "median 300 aa), seed 1, branch substitution rate U(0.01, 0.2), K=6 protein, "
-                 "all 32,640 pairs i<j (+ the 256 self products)")
+WORKLOAD_TEXTS = {
+    "cpu16": ("cpu16: 16 synthetic proteomes x 1,500 proteins (lognormal lengths, median "
+              "300 aa), seed 0, branch substitution rate 0.05, K={k} protein, all {pairs:,} "
+              "pairs i<j (+ the {n} self products)"),
+    "uniform256": ("uniform256: 256 synthetic proteomes x 1,500 proteins (lognormal lengths, "
+                   "median 300 aa), seed 1, branch substitution rate U(0.01, 0.2), K={k} "
+                   "protein, all {pairs:,} pairs i<j (+ the {n} self products)"),
+    "uneven1024": ("uneven1024: 1,024 synthetic proteomes, seed 2, protein counts lognormal "
+                   "(median 1,900, sigma 0.9) clipped to [300, 12,000], lengths lognormal "
+                   "(median 300 aa), branch substitution rate U(0.01, 0.2), K={k} protein, all "
+                   "{pairs:,} pairs i<j (+ the {n} self products)"),
+    "sweep512": ("sweep512: 512 synthetic proteomes, seed 3, protein counts lognormal (median "
+                 "1,900, sigma 0.9) clipped to [300, 12,000], K={k} protein, all {pairs:,} pairs "
+                 "i<j (+ the {n} self products)"),
+}
+
+
+def workload_text(name, k, n):
+    return WORKLOAD_TEXTS[name].format(k=k, pairs=n * (n - 1) // 2, n=n)
 
 
 def _peaks():
@@ -137,7 +153,7 @@ def _barrier_max(value: float, world: int) -> float:
 # CPU baseline (the reference's CPU path, restated in C under oracle/)
 # ----------------------------------------------------------------------------
 
-def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed=0):
+def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed=0, k=6):
     from oracle import oracle as O
     O.lib()
     threads = threads or O.max_threads()
@@ -145,7 +161,7 @@ def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed
     nb = min(len(wl), max(threads, 4))
     ids = rng.choice(len(wl), nb, replace=False)
     t0 = time.perf_counter()
-    vecs = O.java_build_many([wl.get(int(i)) for i in ids], 6, threads=threads)
+    vecs = O.java_build_many([wl.get(int(i)) for i in ids], k, threads=threads)
     t_build = time.perf_counter() - t0
     build_rate = nb / t_build                                      # proteomes / s
     pairs = [(a, b) for a in range(nb) for b in range(a + 1, nb)]
@@ -169,7 +185,7 @@ def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed
 
 
 def plain_path(arena, wl, seq, dev, n_pairs, n_build, peak, sample_pairs=400, sample_builds=16,
-               seed=7):
+               seed=7, k=6):
     """The drop-in path as the reference drives it: one synchronous
     buildCompositionVector per proteome and one synchronous
     compareCompositionVectors per pair (CompositionVectorKernels.java:91-135),
@@ -182,7 +198,7 @@ def plain_path(arena, wl, seq, dev, n_pairs, n_build, peak, sample_pairs=400, sa
     L = _native.load()
     rng = np.random.default_rng(seed)
     maxn = int(arena.nnz.max())
-    ker = CompositionVectorKernels("protein", 6, maxn + 1024, int(wl.lengths().max()), device=dev)
+    ker = CompositionVectorKernels("protein", k, maxn + 1024, int(wl.lengths().max()), device=dev)
     st = ker.stream
     keys = torch.empty(maxn + 1024, dtype=torch.int32, device=dev)
     vals = torch.empty(maxn + 1024, dtype=torch.float32, device=dev)
@@ -248,13 +264,13 @@ def run_reference(args):
     if rank != 0:
         return 0
     from rocket_gb300 import synth
-    wl = synth.workload(WORKLOAD)
+    wl = synth.workload(args.workload, n=args.proteomes)
     n = len(wl)
     n_pairs = n * (n - 1) // 2
     vals = []
     base = None
     for s in range(args.warmup + args.steps):
-        r = cpu_baseline(wl, n_pairs, n, seconds=args.ref_seconds, seed=s)
+        r = cpu_baseline(wl, n_pairs, n, seconds=args.ref_seconds, seed=s, k=args.k)
         if s >= args.warmup:
             vals.append(r["value"])
             base = r
@@ -264,7 +280,7 @@ def run_reference(args):
         "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * n_pairs / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 (java float path)", "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT},
+        "config": {"workload": workload_text(args.workload, args.k, n)},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": base["cores"],
                          "kind": base["kind"], "sample": base["sample"]},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
@@ -290,14 +306,14 @@ def run_ours(args):
     from rocket_gb300 import synth
     from rocket_gb300.engine import BatchBuilder, EngineConfig, PairEngine
 
-    wl = synth.workload(WORKLOAD, n=args.proteomes)
+    wl = synth.workload(args.workload, n=args.proteomes)
     N = len(wl)
     n_pairs = N * (N - 1) // 2
     stream = torch.cuda.current_stream(dev)
     pinned = torch.from_numpy(wl.data).pin_memory()
     seq = torch.empty(pinned.numel(), dtype=torch.uint8, device=dev)
     seq.copy_(pinned)
-    builder = BatchBuilder("protein", 6, device=dev, max_batch=args.max_batch)
+    builder = BatchBuilder("protein", args.k, device=dev, max_batch=args.max_batch)
     cfg = EngineConfig(wshift=args.wshift, fold=args.fold, items_per_cta=args.items_per_cta)
     out = torch.zeros((N, N), dtype=torch.float64, device=dev)
     out_host = torch.zeros((N, N), dtype=torch.float64).pin_memory()
@@ -394,7 +410,7 @@ def run_ours(args):
         "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
         "config": {
-            "workload": WORKLOAD_TEXT,
+            "workload": workload_text(args.workload, args.k, N),
             "parallelism": "replicas" if world > 1 else "single GPU",
             "l2": "flushed between steps (512 MB write, outside the timed events)",
             "nnz_mean": float(nnz.mean()), "nnz_total": int(nnz.sum()),
@@ -421,9 +437,9 @@ def run_ours(args):
         "gpu_launches": int(launches),
     }
     if not args.no_plain:
-        line["plain"] = plain_path(arena, wl, seq, dev, n_pairs, N, peak)
+        line["plain"] = plain_path(arena, wl, seq, dev, n_pairs, N, peak, k=args.k)
     if not args.no_cpu_baseline:
-        cb = cpu_baseline(wl, n_pairs, N, seconds=args.ref_seconds)
+        cb = cpu_baseline(wl, n_pairs, N, seconds=args.ref_seconds, k=args.k)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -530,6 +546,8 @@ def main():
     ap.add_argument("--proteomes", type=int, default=None,
                     help="use only the first N proteomes (small profiling cases)")
     ap.add_argument("--mode", default="allpairs", choices=["allpairs", "serve"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXTS))
+    ap.add_argument("--k", type=int, default=6, help="K-mer length (protein)")
     ap.add_argument("--db", type=int, default=2048, help="serve: database proteomes")
     ap.add_argument("--query-batches", type=int, default=24, help="serve: arriving query batches")
     ap.add_argument("--rate", type=float, default=8.0, help="serve: query batches per second")
