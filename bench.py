@@ -67,12 +67,17 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_per_launch():
-    """DRAM bytes of one pair-kernel launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "allpairs_uniform256_dram.json")
-    if os.path.exists(path):
-        with open(path) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+def _traffic_per_launch(kernel: str, workload: str, wshift: int):
+    """DRAM bytes (read + write) of one pair-kernel launch, from the committed
+    ncu summary of the same kernel, workload and window width (a line
+    `dram_bytes_per_launch = N` in profiles/dram_<kernel>_<workload>_w<shift>.md)."""
+    path = os.path.join(ROOT, "profiles", f"dram_{kernel}_{workload}_w{wshift}.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.strip().startswith("dram_bytes_per_launch"):
+                return float(line.split("=")[1].strip().replace(",", ""))
     return None
 
 
@@ -314,7 +319,8 @@ def run_ours(args):
     seq = torch.empty(pinned.numel(), dtype=torch.uint8, device=dev)
     seq.copy_(pinned)
     builder = BatchBuilder("protein", args.k, device=dev, max_batch=args.max_batch)
-    cfg = EngineConfig(wshift=args.wshift, fold=args.fold, items_per_cta=args.items_per_cta)
+    cfg = EngineConfig(wshift=args.wshift, fold=args.fold, items_per_cta=args.items_per_cta,
+                       tile_rows=args.tile_rows)
     out = torch.zeros((N, N), dtype=torch.float64, device=dev)
     out_host = torch.zeros((N, N), dtype=torch.float64).pin_memory()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -403,7 +409,8 @@ def run_ours(args):
     peak, peak_kind = _peaks()
     k_ms = float(np.mean(kernel_ms))
     achieved = alg_bytes / (k_ms / 1000.0) / 1e9
-    traffic = _traffic_per_launch()
+    kernel_name = "k_allpairs32" if args.tile_rows == 32 else "k_allpairs"
+    traffic = _traffic_per_launch(kernel_name, args.workload, args.wshift)
     line = {
         "metric": "pairwise CV distances/s", "value": value, "unit": "pairs/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -414,7 +421,8 @@ def run_ours(args):
             "parallelism": "replicas" if world > 1 else "single GPU",
             "l2": "flushed between steps (512 MB write, outside the timed events)",
             "nnz_mean": float(nnz.mean()), "nnz_total": int(nnz.sum()),
-            "window_shift": args.wshift, "fold": args.fold, "items": plan.nitems,
+            "window_shift": args.wshift, "tile_rows": args.tile_rows, "fold": args.fold,
+            "items": plan.nitems,
             "segments": plan.S,
         },
         "breakdown_ms": {"build": float(np.mean([p[0] for p in phase_ms])),
@@ -426,7 +434,7 @@ def run_ours(args):
         "roofline": {
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic,
-            "kernel": "k_allpairs",
+            "kernel": kernel_name,
             "note": (f"{peak_kind} peak; algorithmic bytes 8*(nnz_i+nnz_j) per pair = "
                      f"{alg_bytes / 1e9:.1f} GB per launch; frac > 1 = reuse of resident "
                      "vectors in shared memory and L2, not DRAM bandwidth"),
@@ -475,6 +483,7 @@ def run_serve(args):
     db = wl.subset(range(n_db))
     srv = ServingEngine("protein", 6, budget_bytes=args.budget_gb * 1e9, slots=args.slots,
                         max_batch=64, cfg=EngineConfig(wshift=args.wshift, fold=args.fold,
+                                                       tile_rows=args.tile_rows,
                                                        segments=args.segments))
     lens = db.lengths()
     capacity_entries = int(min(np.sum(8 * wl.lengths() + 64),
@@ -537,6 +546,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--wshift", type=int, default=10)
+    ap.add_argument("--tile-rows", type=int, default=32, choices=[16, 32],
+                    help="row vectors per pair-kernel work item (selects the kernel)")
     ap.add_argument("--fold", type=int, default=16)
     ap.add_argument("--items-per-cta", type=int, default=4)
     ap.add_argument("--max-batch", type=int, default=64)

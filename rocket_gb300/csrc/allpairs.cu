@@ -41,11 +41,6 @@ namespace phylo {
 constexpr uint32_t D_STRIDE = 20;  // floats per key record
 
 size_t ap_ring_bytes();
-size_t ap_smem_bytes(uint32_t wshift) {
-    return (((size_t)1 << wshift) + 1) * D_STRIDE * sizeof(float) + ap_ring_bytes();
-}
-
-int ap_max_wshift() { return 11; }
 
 // float index of (key idx, row) in D
 __device__ __forceinline__ uint32_t d_slot(uint32_t idx, uint32_t row) {
@@ -310,20 +305,295 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
     }
 }
 
-cudaError_t ap_prepare(uint32_t wshift, int *ctas_per_sm) {
-    const size_t smem = ap_smem_bytes(wshift);
-    PHYLO_CHECK(cudaFuncSetAttribute(k_allpairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+// ---------------------------------------------------------------------------
+// 32-row items
+// ---------------------------------------------------------------------------
+//
+// The same window scheme with 32 row vectors per item and one 128-byte record
+// (32 row values) per key.  Eight lanes share a column vector and walk the same
+// entries; lane g of the eight holds rows 4g..4g+3, so each entry costs every
+// lane one 16-byte shared load and four FMAs.  Record s keeps rows 4c..4c+3 in
+// its 16-byte chunk c ^ (s & 7): the eight lanes of a column read the eight
+// chunks of one record (one wavefront, never a bank conflict), and the row
+// scatter, where lanes hold different keys of the same row, spreads its stores
+// over eight bank groups.  Column entries are fetched eight at a time (one per
+// lane, three blocks ahead) and passed round the eight lanes by shuffles.  Each
+// lane accumulates its own rows, so a column needs no cross-lane combine.
+
+constexpr uint32_t R32_REC = 32;  // floats per key record
+
+__device__ __forceinline__ uint32_t r32_pos(uint32_t slot, uint32_t row) {
+    return slot * R32_REC + ((((row >> 2) ^ (slot & 7u)) << 2) | (row & 3u));
+}
+
+template <int THREADS>
+struct R32Shape {
+    static constexpr int NW = THREADS / 32;       // warps
+    static constexpr int CPP = NW * 4;            // columns per pass (4 per warp)
+    static constexpr int PASSES = AP_TJ / CPP;    // column passes per window
+    static constexpr int RPW = 32 / NW;           // rows a warp scatters
+    static constexpr int LPR = 32 / RPW;          // lanes per scattered row
+    static constexpr int NPF = RPW;               // prefetched entries per lane (NPF * LPR = 32)
+    static_assert(PASSES * CPP == AP_TJ, "columns per item");
+};
+
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_allpairs32(ApArgs a) {
+    using S = R32Shape<THREADS>;
+    constexpr int PASSES = S::PASSES, RPW = S::RPW, LPR = S::LPR, NPF = S::NPF;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t W = 1u << a.wshift, wmask = W - 1u;
+    float *D = reinterpret_cast<float *>(smem);  // (W + 1) records
+    __shared__ uint32_t s_item;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t g = lane & 7;               // rows 4g..4g+3 on the column side
+    const uint32_t gsrc = lane & ~7u;          // first lane of this column group
+    const uint32_t srow = lane / LPR;          // scatter: row of this lane within the warp
+    const uint32_t sj = lane % LPR;            // scatter: entry offset within the row
+    const uint32_t rr = warp * RPW + srow;     // scatter: row position in the item
+    const uint32_t Rs = a.R + 1;
+
+    for (uint32_t i = threadIdx.x; i < (W + 1) * (R32_REC / 4); i += THREADS)
+        reinterpret_cast<float4 *>(D)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if (it >= a.nitems) break;
+        const ApItem item = a.items[it];
+        const int64_t t_start = clock64();
+
+        // ---- column side: PASSES column vectors per lane group
+        bool has_col[PASSES];
+        uint64_t cbase[PASSES];
+        const uint32_t *cro[PASSES];
+        uint32_t ce[PASSES], c_end[PASSES], blk[PASSES], c_hi_next[PASSES];
+        uint32_t bk0[PASSES], bk1[PASSES], bk2[PASSES];
+        float bv0[PASSES], bv1[PASSES], bv2[PASSES];
+        float acc[PASSES][4], hi[PASSES][4], lo[PASSES][4];
+        uint32_t nacc[PASSES];
+#pragma unroll
+        for (int p = 0; p < PASSES; p++) {
+            const uint32_t jc = p * S::CPP + warp * 4 + (lane >> 3);
+            has_col[p] = jc < item.ncol;
+            const uint32_t cv = has_col[p] ? a.colids[item.col0 + jc] : 0u;
+            cbase[p] = a.col.vec_off[cv];
+            cro[p] = a.col.roff + (uint64_t)cv * Rs;
+            ce[p] = has_col[p] ? __ldg(&cro[p][item.w0]) : 0u;
+            c_end[p] = has_col[p] ? __ldg(&cro[p][item.w1]) : 0u;
+            c_hi_next[p] = has_col[p] ? __ldg(&cro[p][item.w0 + 1]) : 0u;
+            blk[p] = ce[p] & ~7u;
+            const uint32_t e0 = blk[p] + g, e1 = e0 + 8, e2 = e0 + 16;
+            bk0[p] = e0 < c_end[p] ? __ldg(&a.col.keys[cbase[p] + e0]) : 0u;
+            bv0[p] = e0 < c_end[p] ? __ldg(&a.col.vals[cbase[p] + e0]) : 0.f;
+            bk1[p] = e1 < c_end[p] ? __ldg(&a.col.keys[cbase[p] + e1]) : 0u;
+            bv1[p] = e1 < c_end[p] ? __ldg(&a.col.vals[cbase[p] + e1]) : 0.f;
+            bk2[p] = e2 < c_end[p] ? __ldg(&a.col.keys[cbase[p] + e2]) : 0u;
+            bv2[p] = e2 < c_end[p] ? __ldg(&a.col.vals[cbase[p] + e2]) : 0.f;
+#pragma unroll
+            for (int u = 0; u < 4; u++) acc[p][u] = hi[p][u] = lo[p][u] = 0.f;
+            nacc[p] = 0;
+        }
+
+        // ---- row side: this lane scatters row rr
+        const bool has_row = rr < item.nrow;
+        const uint32_t rv = has_row ? a.rowids[item.row0 + rr] : 0u;
+        const uint64_t rbase = a.row.vec_off[rv];
+        const uint32_t *ro = a.row.roff + (uint64_t)rv * Rs;
+        // window offsets of LPR windows, held by the row's lanes
+        uint32_t wb = item.w0;
+        uint32_t r_lo = 0, r_hi = 0;
+        if (has_row) {
+            r_lo = __ldg(&ro[min(wb + sj, a.R)]);
+            r_hi = __ldg(&ro[min(wb + sj + 1, a.R)]);
+        }
+        const int rsrc = (int)(srow * LPR);
+        uint32_t pk[NPF];
+        float pv[NPF];
+        {
+            const uint32_t lo0 = __shfl_sync(0xffffffffu, r_lo, rsrc);
+            const uint32_t hi0 = __shfl_sync(0xffffffffu, r_hi, rsrc);
+#pragma unroll
+            for (int t = 0; t < NPF; t++) {
+                const uint32_t e = lo0 + sj + t * LPR;
+                pk[t] = 0xffffffffu;
+                pv[t] = 0.f;
+                if (has_row && e < hi0) {
+                    pk[t] = __ldg(&a.row.keys[rbase + e]);
+                    pv[t] = __ldg(&a.row.vals[rbase + e]);
+                }
+            }
+        }
+
+        for (uint32_t r = item.w0; r < item.w1; r++) {
+            const int sl = (int)(r - wb);
+            const uint32_t lo_r = __shfl_sync(0xffffffffu, r_lo, rsrc + sl);
+            const uint32_t hi_r = __shfl_sync(0xffffffffu, r_hi, rsrc + sl);
+            // scatter window r of row rr
+            uint32_t ck[NPF];
+#pragma unroll
+            for (int t = 0; t < NPF; t++) {
+                ck[t] = pk[t];
+                if (pk[t] != 0xffffffffu) D[r32_pos(pk[t] & wmask, rr)] = pv[t];
+            }
+            if (has_row) {
+                for (uint32_t e = lo_r + 32 + sj; e < hi_r; e += LPR) {
+                    const uint32_t key = __ldg(&a.row.keys[rbase + e]);
+                    D[r32_pos(key & wmask, rr)] = __ldg(&a.row.vals[rbase + e]);
+                }
+            }
+            // prefetch the next window's offsets and first entries
+            if (r + 1 < item.w1) {
+                if (r + 1 - wb >= (uint32_t)LPR) {
+                    wb = r + 1;
+                    if (has_row) {
+                        r_lo = __ldg(&ro[min(wb + sj, a.R)]);
+                        r_hi = __ldg(&ro[min(wb + sj + 1, a.R)]);
+                    }
+                }
+                const int sn = (int)(r + 1 - wb);
+                const uint32_t nlo = __shfl_sync(0xffffffffu, r_lo, rsrc + sn);
+                const uint32_t nhi = __shfl_sync(0xffffffffu, r_hi, rsrc + sn);
+#pragma unroll
+                for (int t = 0; t < NPF; t++) {
+                    const uint32_t e = nlo + sj + t * LPR;
+                    pk[t] = 0xffffffffu;
+                    if (has_row && e < nhi) {
+                        pk[t] = __ldg(&a.row.keys[rbase + e]);
+                        pv[t] = __ldg(&a.row.vals[rbase + e]);
+                    }
+                }
+            }
+            uint32_t c_hi[PASSES];
+#pragma unroll
+            for (int p = 0; p < PASSES; p++) {
+                c_hi[p] = c_hi_next[p];
+                if (has_col[p] && r + 2 <= a.R) c_hi_next[p] = __ldg(&cro[p][r + 2]);
+            }
+            __syncthreads();
+            // column entries of window r
+#pragma unroll
+            for (int p = 0; p < PASSES; p++) {
+                const uint32_t cnt = c_hi[p] - ce[p];  // 0 without a column
+                const uint32_t maxc = __reduce_max_sync(0xffffffffu, cnt);
+                for (uint32_t t = 0; t < maxc; t++) {
+                    const bool act = t < cnt;
+                    const uint32_t ee = ce[p] + t;
+                    if (act && ee >= blk[p] + 8) {
+                        blk[p] += 8;
+                        bk0[p] = bk1[p]; bv0[p] = bv1[p];
+                        bk1[p] = bk2[p]; bv1[p] = bv2[p];
+                        const uint32_t e2 = blk[p] + 16 + g;
+                        if (e2 < c_end[p]) {
+                            bk2[p] = __ldg(&a.col.keys[cbase[p] + e2]);
+                            bv2[p] = __ldg(&a.col.vals[cbase[p] + e2]);
+                        }
+                    }
+                    const int src = (int)(gsrc | (ee & 7u));
+                    const uint32_t k = __shfl_sync(0xffffffffu, bk0[p], src);
+                    const float v = __shfl_sync(0xffffffffu, bv0[p], src);
+                    const uint32_t slot = act ? (k & wmask) : W;
+                    const float b = act ? v : 0.f;
+                    const float4 q = *reinterpret_cast<const float4 *>(
+                        D + slot * R32_REC + ((g ^ (slot & 7u)) << 2));
+                    acc[p][0] = __fmaf_rn(q.x, b, acc[p][0]);
+                    acc[p][1] = __fmaf_rn(q.y, b, acc[p][1]);
+                    acc[p][2] = __fmaf_rn(q.z, b, acc[p][2]);
+                    acc[p][3] = __fmaf_rn(q.w, b, acc[p][3]);
+                    if (++nacc[p] >= a.fold) {
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            float s2, e2;
+                            two_sum(hi[p][u], acc[p][u], s2, e2);
+                            hi[p][u] = s2;
+                            lo[p][u] = __fadd_rn(lo[p][u], e2);
+                            acc[p][u] = 0.f;
+                        }
+                        nacc[p] = 0;
+                    }
+                }
+                ce[p] += cnt;
+            }
+            __syncthreads();
+            // clear window r of row rr
+#pragma unroll
+            for (int t = 0; t < NPF; t++)
+                if (ck[t] != 0xffffffffu) D[r32_pos(ck[t] & wmask, rr)] = 0.f;
+            if (has_row) {
+                for (uint32_t e = lo_r + 32 + sj; e < hi_r; e += LPR) {
+                    const uint32_t key = __ldg(&a.row.keys[rbase + e]);
+                    D[r32_pos(key & wmask, rr)] = 0.f;
+                }
+            }
+            __syncwarp();
+        }
+        // fold and write: lane g of column jc owns rows 4g..4g+3
+        FF *dst = a.part + (uint64_t)item.part * (32 * AP_TJ);
+#pragma unroll
+        for (int p = 0; p < PASSES; p++) {
+            const uint32_t jc = p * S::CPP + warp * 4 + (lane >> 3);
+            if (!has_col[p]) continue;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                float s2, e2;
+                two_sum(hi[p][u], acc[p][u], s2, e2);
+                FF v;
+                two_sum(s2, __fadd_rn(lo[p][u], e2), v.hi, v.lo);
+                dst[(4 * g + u) * AP_TJ + jc] = v;
+            }
+        }
+        if (a.item_cycles && threadIdx.x == 0) a.item_cycles[it] = clock64() - t_start;
+    }
+}
+
+// 32-row kernel: 512 threads (one pass over 64 columns) when the table leaves
+// room for one CTA per SM, else 256 threads (two passes) and two CTAs per SM.
+static size_t r32_smem_bytes(uint32_t wshift) {
+    return (((size_t)1 << wshift) + 1) * R32_REC * sizeof(float);
+}
+static bool r32_wide(uint32_t wshift) { return r32_smem_bytes(wshift) > 100 * 1024; }
+
+size_t ap_smem_bytes(uint32_t wshift, int tile_rows) {
+    if (tile_rows == 32) return r32_smem_bytes(wshift);
+    return (((size_t)1 << wshift) + 1) * D_STRIDE * sizeof(float) + ap_ring_bytes();
+}
+
+int ap_max_wshift(int tile_rows) { return tile_rows == 32 ? 10 : 11; }
+
+int ap_threads(uint32_t wshift, int tile_rows) {
+    if (tile_rows == 32) return r32_wide(wshift) ? 512 : 256;
+    return AP_THREADS;
+}
+
+cudaError_t ap_prepare(uint32_t wshift, int tile_rows, int *ctas_per_sm) {
+    const size_t smem = ap_smem_bytes(wshift, tile_rows);
+    const void *fn;
+    if (tile_rows == 32)
+        fn = r32_wide(wshift) ? (const void *)k_allpairs32<512, 1> : (const void *)k_allpairs32<256, 2>;
+    else
+        fn = (const void *)k_allpairs;
+    PHYLO_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (ctas_per_sm) {
         int n = 0;
-        PHYLO_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_allpairs, AP_THREADS, smem));
+        PHYLO_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, fn, ap_threads(wshift, tile_rows), smem));
         *ctas_per_sm = n;
     }
     return cudaSuccess;
 }
 
-cudaError_t ap_launch(const ApArgs &a, int grid, cudaStream_t st) {
-    k_allpairs<<<grid, AP_THREADS, ap_smem_bytes(a.wshift), st>>>(a);
+cudaError_t ap_launch(const ApArgs &a, int tile_rows, int grid, cudaStream_t st) {
+    const size_t smem = ap_smem_bytes(a.wshift, tile_rows);
+    if (tile_rows == 32) {
+        if (r32_wide(a.wshift))
+            k_allpairs32<512, 1><<<grid, 512, smem, st>>>(a);
+        else
+            k_allpairs32<256, 2><<<grid, 256, smem, st>>>(a);
+    } else {
+        k_allpairs<<<grid, AP_THREADS, smem, st>>>(a);
+    }
     return cudaGetLastError();
 }
 
@@ -384,13 +654,14 @@ __global__ void k_ap_reduce(ApReduceArgs r) {
     const uint32_t c = threadIdx.x;
     if (c >= t.ncol) return;
     const uint32_t colid = r.colids[t.col0 + c];
-    const FF *base = r.part + (uint64_t)blockIdx.x * r.S * (AP_TI * AP_TJ);
+    const uint64_t blk = (uint64_t)r.ti * AP_TJ;  // float pairs per partial block
+    const FF *base = r.part + (uint64_t)blockIdx.x * r.S * blk;
     for (uint32_t i = 0; i < t.nrow; i++) {
         const uint32_t rowpos = t.row0 + i, colpos = t.col0 + c;
         if (r.upper && !(rowpos < colpos)) continue;
         DD acc = {0.0, 0.0};
         for (uint32_t s = 0; s < r.S; s++) {
-            const FF p = base[(uint64_t)s * (AP_TI * AP_TJ) + i * AP_TJ + c];
+            const FF p = base[(uint64_t)s * blk + i * AP_TJ + c];
             dd_add(acc, (double)p.hi);
             dd_add(acc, (double)p.lo);
         }

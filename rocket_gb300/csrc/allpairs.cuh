@@ -36,15 +36,18 @@ struct ApArgs {
     const ApItem *items;
     uint32_t nitems;
     uint32_t *counter;         // work counter (zeroed before launch)
-    FF *part;                  // [parts][AP_TI][AP_TJ]
+    FF *part;                  // [parts][tile rows][AP_TJ]
     uint32_t fold;             // products per accumulator between compensated folds
     int64_t *item_cycles;      // optional per-item clock64 durations (may be null)
 };
 
-size_t ap_smem_bytes(uint32_t wshift);
-int ap_max_wshift();
-cudaError_t ap_prepare(uint32_t wshift, int *ctas_per_sm);
-cudaError_t ap_launch(const ApArgs &a, int grid, cudaStream_t st);
+// tile_rows selects the kernel: 16 (80-byte records, four lanes per column) or
+// 32 (128-byte swizzled records, eight lanes per column).
+size_t ap_smem_bytes(uint32_t wshift, int tile_rows);
+int ap_max_wshift(int tile_rows);
+int ap_threads(uint32_t wshift, int tile_rows);
+cudaError_t ap_prepare(uint32_t wshift, int tile_rows, int *ctas_per_sm);
+cudaError_t ap_launch(const ApArgs &a, int tile_rows, int grid, cudaStream_t st);
 
 // window index: roff[v][r] = number of entries of vector v with key < r << wshift
 cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
@@ -58,9 +61,9 @@ struct ApTile {
     uint32_t row0, nrow, col0, ncol;
 };
 struct ApReduceArgs {
-    const FF *part;
+    const FF *part;            // blocks of ti x AP_TJ float pairs
     const ApTile *tiles;
-    uint32_t ntiles, S;
+    uint32_t ntiles, S, ti;
     const uint32_t *rowids, *colids;
     double *out;
     uint64_t ldc;

@@ -29,7 +29,7 @@ import torch
 from . import _native
 from ._native import check
 
-AP_TI = 16
+AP_TI = 32          # default rows per work item (16 or 32: selects the pair kernel)
 AP_TJ = 64
 NSYM = {"protein": 21, "DNA": 4}
 
@@ -228,6 +228,7 @@ class PairPlan:
 @dataclass
 class EngineConfig:
     wshift: int = 10
+    tile_rows: int = AP_TI   # 16 or 32 row vectors per work item
     fold: int = 16
     items_per_cta: int = 4
     min_windows_per_item: int = 64
@@ -242,7 +243,7 @@ class PairEngine:
         self.L = _native.load()
         self.device = arena.keys.device
         ctas = ctypes.c_int(0)
-        check(self.L.phyloPairsPrepare(self.cfg.wshift, ctypes.byref(ctas)))
+        check(self.L.phyloPairsPrepare(self.cfg.wshift, self.cfg.tile_rows, ctypes.byref(ctas)))
         self.ctas_per_sm = max(1, ctas.value)
         props = torch.cuda.get_device_properties(self.device)
         self.sms = props.multi_processor_count
@@ -298,7 +299,7 @@ class PairEngine:
             cn = col_nnz[colids[c0:c0 + nc]]
             # linear model: 16 products per column entry + row scatter/clear
             # + a fixed cost per window
-            e_tile = AP_TI * cn.sum() + 2.0 * rn.sum() + 64.0 * R
+            e_tile = self.cfg.tile_rows * cn.sum() + 2.0 * rn.sum() + 64.0 * R
             # nnz-product estimate: sum over the tile's pairs of sqrt(nnz_i * nnz_j)
             e_prod = float(np.sqrt(np.outer(rn, cn)).sum())
             for s in range(S):
@@ -327,8 +328,9 @@ class PairEngine:
         perm = ids[order]
         N = len(perm)
         tiles = []
-        for r0 in range(0, N, AP_TI):
-            nr = min(AP_TI, N - r0)
+        ti = self.cfg.tile_rows
+        for r0 in range(0, N, ti):
+            nr = min(ti, N - r0)
             c = r0 + 1
             while c < N:
                 nc = min(AP_TJ, N - c)
@@ -347,8 +349,9 @@ class PairEngine:
         rows = rows[np.argsort(-a.nnz[rows], kind="stable")]
         cols = cols[np.argsort(-ca.nnz[cols], kind="stable")]
         tiles = []
-        for r0 in range(0, len(rows), AP_TI):
-            nr = min(AP_TI, len(rows) - r0)
+        ti = self.cfg.tile_rows
+        for r0 in range(0, len(rows), ti):
+            nr = min(ti, len(rows) - r0)
             for c0 in range(0, len(cols), AP_TJ):
                 tiles.append((r0, nr, c0, min(AP_TJ, len(cols) - c0)))
         return self._finish_plan(rows, cols, tiles, False, False, ldc, len(rows) * len(cols),
@@ -356,7 +359,7 @@ class PairEngine:
 
     # -- execution -------------------------------------------------------------
     def _parts(self, plan: PairPlan) -> torch.Tensor:
-        need = plan.ntiles * plan.S * AP_TI * AP_TJ * 2
+        need = plan.ntiles * plan.S * self.cfg.tile_rows * AP_TJ * 2
         if self.part is None or self.part.numel() < need:
             self.part = torch.empty(need, dtype=torch.float32, device=self.device)
         return self.part
@@ -379,12 +382,13 @@ class PairEngine:
             _p(ca.vec_off), _p(ca.roff), a.R, self.cfg.wshift,
             _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems, _p(self.counter),
             _p(part), self.cfg.fold, _p(item_cycles) if item_cycles is not None else 0,
-            self.grid))
+            self.cfg.tile_rows, self.grid))
         if events is not None:
             events[1].record(s_obj)
         check(self.L.phyloPairsReduce(
-            st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, _p(plan.rowids), _p(plan.colids),
-            _p(out), plan.ldc, int(plan.upper), int(plan.mirror)))
+            st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, self.cfg.tile_rows,
+            _p(plan.rowids), _p(plan.colids), _p(out), plan.ldc, int(plan.upper),
+            int(plan.mirror)))
         self.launches += 3  # counter fill, pair kernel, reduction
         if diagonal and plan.upper:
             maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
@@ -509,12 +513,12 @@ def tune_key(arena: Arena, n_rows: int, n_cols: int) -> str:
 
 
 TUNE_SPACE = [
-    dict(wshift=10, fold=16, items_per_cta=4),
-    dict(wshift=10, fold=16, items_per_cta=2),
-    dict(wshift=10, fold=16, items_per_cta=8),
-    dict(wshift=9, fold=16, items_per_cta=4),
-    dict(wshift=11, fold=16, items_per_cta=4),
-    dict(wshift=10, fold=8, items_per_cta=4),
+    dict(wshift=10, tile_rows=32, fold=16, items_per_cta=4),
+    dict(wshift=10, tile_rows=32, fold=16, items_per_cta=2),
+    dict(wshift=10, tile_rows=32, fold=16, items_per_cta=8),
+    dict(wshift=9, tile_rows=32, fold=16, items_per_cta=4),
+    dict(wshift=10, tile_rows=16, fold=16, items_per_cta=4),
+    dict(wshift=11, tile_rows=16, fold=16, items_per_cta=4),
 ]
 
 

@@ -37,7 +37,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .engine import AP_TI, AP_TJ, Arena, BatchBuilder, EngineConfig, PairEngine, key_limit
+from .engine import AP_TJ, Arena, BatchBuilder, EngineConfig, PairEngine, key_limit
 from .synth import Proteomes
 
 
@@ -241,8 +241,9 @@ class ServingEngine:
                                                  min(nq, self.max_batch), int(cand)))
         staged = float(np.sum(8 * lens + 64)) * 8.0
         roff = nq * (self.db.R + 1) * 4.0
-        tiles = math.ceil(nq / AP_TI) * math.ceil(max(db_n, 1) / AP_TJ)
-        parts = tiles * self.cfg.segments * AP_TI * AP_TJ * 8.0
+        ti = self.cfg.tile_rows
+        tiles = math.ceil(nq / ti) * math.ceil(max(db_n, 1) / AP_TJ)
+        parts = tiles * self.cfg.segments * ti * AP_TJ * 8.0
         out = nq * max(db_n, 1) * 8.0
         return scratch + staged + roff + parts + out
 

@@ -29,10 +29,20 @@ def small():
     return p, arena, oracle_matrix(p)
 
 
-@pytest.mark.parametrize("wshift,fold", [(10, 16), (9, 8), (11, 16)])
-def test_allpairs_matches_fp64(small, wshift, fold):
+@pytest.fixture(scope="module")
+def many():
+    """90 small proteomes: several 32-row groups and 64-column tiles, ragged edges."""
+    p = synth.workload("uneven1024", n=90, scale=0.01)
+    d = torch.from_numpy(p.data).cuda()
+    arena = BatchBuilder("protein", 6).build(d, p.offsets)
+    return p, arena, oracle_matrix(p)
+
+
+@pytest.mark.parametrize("wshift,fold,rows", [(10, 16, 16), (9, 8, 16), (11, 16, 16),
+                                              (10, 16, 32), (9, 16, 32), (10, 8, 32)])
+def test_allpairs_matches_fp64(small, wshift, fold, rows):
     p, arena, C_ref = small
-    eng = PairEngine(arena, EngineConfig(wshift=wshift, fold=fold))
+    eng = PairEngine(arena, EngineConfig(wshift=wshift, fold=fold, tile_rows=rows))
     eng.ensure_index()
     plan = eng.plan_triangle()
     out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
@@ -45,6 +55,32 @@ def test_allpairs_matches_fp64(small, wshift, fold):
     out2 = torch.zeros_like(out)
     eng.run(plan, out2)
     assert torch.equal(out, out2)
+
+
+@pytest.mark.parametrize("wshift,rows", [(10, 32), (9, 32), (10, 16)])
+def test_allpairs_many_tiles(many, wshift, rows):
+    p, arena, C_ref = many
+    eng = PairEngine(arena, EngineConfig(wshift=wshift, tile_rows=rows))
+    eng.ensure_index()
+    plan = eng.plan_triangle()
+    assert plan.ntiles > 2
+    out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+    eng.run(plan, out)
+    err = np.abs(out.cpu().numpy() - C_ref) / 2
+    assert err.max() <= 1e-6, err.max()
+
+
+def test_tile_rows_agree(many):
+    """Both kernels compute the same C to within the accumulation bound."""
+    p, arena, _ = many
+    outs = []
+    for rows in (16, 32):
+        eng = PairEngine(arena, EngineConfig(wshift=10, tile_rows=rows))
+        eng.ensure_index()
+        out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+        eng.run(eng.plan_triangle(), out)
+        outs.append(out.cpu().numpy())
+    assert np.abs(outs[0] - outs[1]).max() <= 2.2e-6
 
 
 def test_rectangle_plan(small):
