@@ -192,6 +192,17 @@ int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int 
 /* Scratch bytes phyloSelfDot needs. */
 long phyloSelfDotPartBytes(int num_vectors, long max_vector_len);
 
+/* Dense key ranks (no counterpart in the reference: an input transform of
+ * the batched pair path).  d_rank_keys[e] = number of distinct keys of the
+ * num_vectors vectors below d_keys[e] -- a strictly increasing map, so the
+ * pair kernel gives the same products on ranks as on keys, over a denser key
+ * space; padding keys 0xFFFFFFFF are kept.  key_limit bounds every key (A^K);
+ * d_union_size (uint64, device) receives the union size.  Asynchronous. */
+long phyloKeyRankScratch(long key_limit);
+int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
+                  uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
+                  uintptr_t d_rank_keys, uintptr_t d_union_size);
+
 /* Scratch bytes of phyloComparePairsMany for num_pairs pairs and at most
  * max_tiles merge tiles (sum over pairs of ceil((nl + nr) / 4096)). */
 long phyloComparePairsManyScratch(int num_pairs, long max_tiles);

@@ -102,6 +102,11 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloComparePairAsync.argtypes = [c_ptr, c_ptr, c_long, c_ptr, c_ptr, c_int, c_ptr, c_ptr,
                                         c_int, c_ptr]
     L.phyloComparePairAsync.restype = c_int
+    L.phyloKeyRankScratch.argtypes = [c_long]
+    L.phyloKeyRankScratch.restype = c_long
+    L.phyloKeyRanks.argtypes = [c_ptr, c_ptr, c_long, c_long, c_ptr, c_ptr, c_int, c_long, c_ptr,
+                                c_ptr]
+    L.phyloKeyRanks.restype = c_int
     L.phyloComparePairsManyScratch.argtypes = [c_int, c_long]
     L.phyloComparePairsManyScratch.restype = c_long
     L.phyloComparePairsMany.argtypes = [c_ptr, c_ptr, c_long] + [c_ptr] * 10 + [c_int, c_long, c_ptr]
@@ -115,7 +120,8 @@ EXPORTED = [
     "phyloBuildBatchCounts", "phyloBuildLaunchesPerBatch", "phyloWindowIndex",
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsThreads", "phyloPairsLaunch",
     "phyloPairsReduce",
-    "phyloSelfDot", "phyloSelfDotPartBytes", "phyloComparePairsManyScratch",
+    "phyloSelfDot", "phyloSelfDotPartBytes", "phyloKeyRankScratch", "phyloKeyRanks",
+    "phyloComparePairsManyScratch",
     "phyloComparePairsMany", "phyloComparePairAsync",
 ]
 

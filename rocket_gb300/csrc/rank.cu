@@ -1,0 +1,145 @@
+// rank.cu -- dense key ranks: every key of a set of vectors replaced by its
+// rank in the union of the set's keys.
+//
+// The window pair kernel cuts the key space into windows of W keys; its cost
+// per window (barriers, the row scatter, ragged column groups) is paid whether
+// a window holds many entries or few.  Protein keys use a small part of their
+// space (K=6: ~31 M of 21^6 = 86 M keys in the union of 64 proteomes; K=7: a
+// far smaller part of 21^7), so the pair kernel runs on ranks instead: a
+// strictly increasing map, so each vector stays sorted, equal keys stay equal
+// and different keys stay different -- the products and their order are those
+// of the raw keys, only the windows are denser.
+//
+//   k_rank_mark     union bitmap of the keys (warp-combined atomicOr)
+//   k_rank_reduce / k_scan_partials / k_rank_prefix
+//                   exclusive prefix of the bitmap's population per 32-bit word
+//   k_rank_apply    rank = prefix[key / 32] + popc(word & bits below key)
+#include "rank.cuh"
+#include "scan.cuh"
+
+namespace phylo {
+
+constexpr uint32_t RK_SLICE = 16384;  // entries per CTA (mark / apply)
+constexpr uint32_t RK_THREADS = 256;
+
+// grid = (slices, N)
+__global__ void __launch_bounds__(RK_THREADS) k_rank_mark(const uint32_t *__restrict__ keys,
+                                                          const uint64_t *__restrict__ vec_off,
+                                                          uint32_t *bits) {
+    const uint32_t v = blockIdx.y;
+    const uint64_t b = vec_off[v];
+    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);
+    const uint32_t e0 = blockIdx.x * RK_SLICE;
+    if (e0 >= n) return;
+    const uint32_t e1 = min(n, e0 + RK_SLICE);
+    for (uint32_t base = e0; base < e1; base += RK_THREADS) {
+        const uint32_t e = base + threadIdx.x;
+        const uint32_t key = e < e1 ? keys[b + e] : 0xffffffffu;
+        const bool valid = key != 0xffffffffu;  // padding
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            const uint32_t w = key >> 5;
+            const unsigned peers = __match_any_sync(act, w);
+            const uint32_t m = __reduce_or_sync(peers, 1u << (key & 31u));
+            if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && (__ldcg(&bits[w]) & m) != m)
+                atomicOr(&bits[w], m);
+        }
+    }
+}
+
+// Population of SCAN_TILE words per CTA -> partials[cta].
+__global__ void __launch_bounds__(SCAN_THREADS) k_rank_reduce(const uint32_t *__restrict__ bits,
+                                                              uint64_t nwords, uint64_t *partials) {
+    __shared__ uint64_t sw[SCAN_THREADS / 32 + 1];
+    const uint64_t first = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint64_t s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++)
+        if (first + i < nwords) s += __popc(bits[first + i]);
+    uint64_t tot;
+    block_excl_scan_u64<SCAN_THREADS>(s, sw, &tot);
+    if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+}
+
+// prefix[w] = keys of the union below word w; *total = union size.
+__global__ void __launch_bounds__(SCAN_THREADS) k_rank_prefix(const uint32_t *__restrict__ bits,
+                                                              uint64_t nwords,
+                                                              const uint64_t *__restrict__ partials,
+                                                              uint32_t *prefix, uint64_t *total) {
+    __shared__ uint64_t sw[SCAN_THREADS / 32 + 1];
+    const uint64_t first = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t c[SCAN_ITEMS];
+    uint64_t s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        c[i] = first + i < nwords ? (uint32_t)__popc(bits[first + i]) : 0u;
+        s += c[i];
+    }
+    uint64_t tot;
+    uint64_t ex = block_excl_scan_u64<SCAN_THREADS>(s, sw, &tot) + partials[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        if (first + i < nwords) prefix[first + i] = (uint32_t)ex;
+        ex += c[i];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total = partials[gridDim.x];
+}
+
+// grid = (slices, N); padding keys stay 0xffffffff.
+__global__ void __launch_bounds__(RK_THREADS) k_rank_apply(const uint32_t *__restrict__ keys,
+                                                           const uint64_t *__restrict__ vec_off,
+                                                           const uint32_t *__restrict__ bits,
+                                                           const uint32_t *__restrict__ prefix,
+                                                           uint32_t *ranks) {
+    const uint32_t v = blockIdx.y;
+    const uint64_t b = vec_off[v];
+    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);
+    const uint32_t e0 = blockIdx.x * RK_SLICE;
+    if (e0 >= n) return;
+    const uint32_t e1 = min(n, e0 + RK_SLICE);
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += RK_THREADS) {
+        const uint32_t key = keys[b + e];
+        uint32_t r = 0xffffffffu;
+        if (key != 0xffffffffu) {
+            const uint32_t w = key >> 5;
+            r = __ldg(&prefix[w]) + (uint32_t)__popc(__ldg(&bits[w]) & ((1u << (key & 31u)) - 1u));
+        }
+        ranks[b + e] = r;
+    }
+}
+
+static uint64_t rank_words(uint64_t key_limit) { return div_up(key_limit ? key_limit : 1, 32); }
+
+size_t rank_scratch_bytes(uint64_t key_limit) {
+    const uint64_t nw = rank_words(key_limit);
+    const uint64_t nb = div_up(nw, SCAN_TILE);
+    return scratch_bytes<uint32_t>(nw) + scratch_bytes<uint32_t>(nw) +
+           scratch_bytes<uint64_t>(nb + 1) + scratch_bytes<uint64_t>(1);
+}
+
+cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N, uint64_t max_len,
+                      uint64_t key_limit, void *scratch, size_t scratch_size, uint32_t *ranks,
+                      uint64_t *d_union, cudaStream_t st) {
+    const uint64_t nw = rank_words(key_limit);
+    const uint64_t nb = div_up(nw, SCAN_TILE);
+    Scratch sc(scratch, scratch_size);
+    uint32_t *bits = sc.take<uint32_t>(nw);
+    uint32_t *prefix = sc.take<uint32_t>(nw);
+    uint64_t *partials = sc.take<uint64_t>(nb + 1);
+    uint64_t *total = sc.take<uint64_t>(1);
+    if (!total) return cudaErrorInvalidValue;
+    PHYLO_CHECK(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * nw, st));
+    const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, RK_SLICE);
+    if (N) k_rank_mark<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, bits);
+    k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials);
+    k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
+    k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials, prefix, total);
+    if (N) k_rank_apply<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, bits, prefix, ranks);
+    if (d_union) PHYLO_CHECK(cudaMemcpyAsync(d_union, total, sizeof(uint64_t),
+                                             cudaMemcpyDeviceToDevice, st));
+    return cudaGetLastError();
+}
+
+int key_ranks_launches() { return 6; }  // memset not counted: mark, reduce, scan, prefix, apply, copy
+
+}  // namespace phylo

@@ -29,7 +29,7 @@ import torch
 from . import _native
 from ._native import check
 
-AP_TI = 32          # default rows per work item (16 or 32: selects the pair kernel)
+AP_TI = 16          # default rows per work item (16 or 32: selects the pair kernel)
 AP_TJ = 64
 NSYM = {"protein": 21, "DNA": 4}
 
@@ -67,6 +67,22 @@ class Arena:
     wshift: int = 0
     R: int = 0
     indexed: int = 0            # vectors covered by roff
+    rkeys: Optional[torch.Tensor] = None   # dense key ranks (pair kernel input), or None
+    rank_limit: int = 0         # union size of the ranked vectors
+    ranked: int = 0             # vectors covered by rkeys (ranks of all of them change together)
+    index_on_ranks: bool = False
+
+    def index_state(self):
+        return (self.roff, self.wshift, self.R, self.indexed, self.rkeys, self.rank_limit,
+                self.ranked, self.index_on_ranks)
+
+    def restore_index(self, st) -> None:
+        (self.roff, self.wshift, self.R, self.indexed, self.rkeys, self.rank_limit, self.ranked,
+         self.index_on_ranks) = st
+
+    def pair_keys(self) -> torch.Tensor:
+        """The keys the window index and the pair kernel read."""
+        return self.rkeys if self.index_on_ranks else self.keys
 
     @property
     def used(self) -> int:
@@ -79,6 +95,7 @@ class Arena:
         self.off = np.zeros(1, np.int64)
         self.norms = np.zeros(0, np.float64)
         self.indexed = 0
+        self.ranked = 0
         return self
 
     def vector(self, v: int):
@@ -234,6 +251,7 @@ class EngineConfig:
     min_windows_per_item: int = 64
     segments: int = 0        # key segments per tile; 0 = chosen from the plan size.  A fixed
                              # value makes each pair's arithmetic independent of the plan.
+    compress: bool = True    # run the pair kernel on dense key ranks (one arena only)
 
 
 class PairEngine:
@@ -256,13 +274,24 @@ class PairEngine:
 
     # -- window index ------------------------------------------------------
     def ensure_index(self, stream=None) -> None:
-        """Builds (or extends to newly appended vectors) the window index."""
+        """Builds (or extends to newly appended vectors) the window index; with
+        ``compress``, first replaces the keys by their ranks in the union of the
+        arena's keys (recomputed for all vectors when vectors were appended)."""
         a = self.arena
         W = 1 << self.cfg.wshift
-        R = (key_limit(a.alphabet, a.k) + W - 1) // W
-        if a.roff is None or a.wshift != self.cfg.wshift:
+        st = _stream_handle(stream)
+        if self.cfg.compress:
+            if a.rkeys is None or a.ranked != a.n:
+                self._rank(a, st)
+            limit = a.rank_limit
+        else:
+            limit = key_limit(a.alphabet, a.k)
+        R = max(1, (limit + W - 1) // W)
+        if (a.roff is None or a.wshift != self.cfg.wshift or a.R != R
+                or a.index_on_ranks != self.cfg.compress):
             a.roff = torch.empty((max(a.n, 1), R + 1), dtype=torch.int32, device=self.device)
             a.wshift, a.R, a.indexed = self.cfg.wshift, R, 0
+            a.index_on_ranks = self.cfg.compress
         if a.roff.shape[0] < a.n:
             new = torch.empty((int(a.n * 1.5) + 1, R + 1), dtype=torch.int32, device=self.device)
             new[:a.roff.shape[0]].copy_(a.roff)
@@ -270,10 +299,27 @@ class PairEngine:
         if a.indexed < a.n:
             maxlen = int(np.max(np.diff(a.off[a.indexed:a.n + 1])))
             check(self.L.phyloWindowIndex(
-                _stream_handle(stream), _p(a.keys), _p(a.vec_off[a.indexed:]), a.n - a.indexed,
+                st, _p(a.pair_keys()), _p(a.vec_off[a.indexed:]), a.n - a.indexed,
                 self.cfg.wshift, R, maxlen, _p(a.roff[a.indexed])))
             self.launches += 1
             a.indexed = a.n
+
+    def _rank(self, a: Arena, st: int) -> None:
+        limit = key_limit(a.alphabet, a.k)
+        nb = int(self.L.phyloKeyRankScratch(limit))
+        if getattr(self, "_rank_scratch", None) is None or self._rank_scratch.numel() < nb:
+            self._rank_scratch = torch.empty(nb, dtype=torch.uint8, device=self.device)
+        if a.rkeys is None or a.rkeys.numel() < a.keys.numel():
+            a.rkeys = torch.empty(a.keys.numel(), dtype=torch.int32, device=self.device)
+        union = torch.zeros(1, dtype=torch.int64, device=self.device)
+        maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
+        check(self.L.phyloKeyRanks(st, _p(self._rank_scratch), self._rank_scratch.numel(), limit,
+                                   _p(a.keys), _p(a.vec_off), a.n, maxlen, _p(a.rkeys),
+                                   _p(union)))
+        self.launches += 6
+        a.rank_limit = int(union.cpu().item())  # synchronises: the window count depends on it
+        a.ranked = a.n
+        a.indexed = 0  # every vector's ranks may have changed
 
     # -- planning ------------------------------------------------------------
     def _segments(self, ntiles: int) -> int:
@@ -377,9 +423,12 @@ class PairEngine:
         if events is not None:
             events[0].record(s_obj)
         ca = col_arena if col_arena is not None else a
+        if ca is not a and (a.index_on_ranks or ca.index_on_ranks):
+            raise ValueError("dense key ranks need rows and columns in the same arena "
+                             "(EngineConfig(compress=False) for two arenas)")
         check(self.L.phyloPairsLaunch(
-            st, _p(a.keys), _p(a.values), _p(a.vec_off), _p(a.roff), _p(ca.keys), _p(ca.values),
-            _p(ca.vec_off), _p(ca.roff), a.R, self.cfg.wshift,
+            st, _p(a.pair_keys()), _p(a.values), _p(a.vec_off), _p(a.roff), _p(ca.pair_keys()),
+            _p(ca.values), _p(ca.vec_off), _p(ca.roff), a.R, self.cfg.wshift,
             _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems, _p(self.counter),
             _p(part), self.cfg.fold, _p(item_cycles) if item_cycles is not None else 0,
             self.cfg.tile_rows, self.grid))
@@ -547,9 +596,7 @@ def autotune(arena: Arena, ids=None, space=None, repeats: int = 2, use_cache: bo
     out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device=arena.keys.device)
     for cfg in space:
         eng = PairEngine(arena, EngineConfig(**cfg))
-        saved = (arena.roff, arena.wshift, arena.R, arena.indexed)
-        if arena.wshift != cfg["wshift"]:
-            arena.roff, arena.indexed = None, 0
+        saved = arena.index_state()
         eng.ensure_index()
         plan = eng.plan_triangle(ids)
         eng.run(plan, out, diagonal=False)
@@ -564,8 +611,7 @@ def autotune(arena: Arena, ids=None, space=None, repeats: int = 2, use_cache: bo
             torch.cuda.synchronize()
             best = min(best, e0.elapsed_time(e1))
         results.append(dict(cfg, algorithm="window", ms=best))
-        if arena.wshift != saved[1]:
-            arena.roff, arena.wshift, arena.R, arena.indexed = saved
+        arena.restore_index(saved)
         if verbose:
             print(results[-1], flush=True)
     if include_merge:

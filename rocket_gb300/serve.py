@@ -27,6 +27,7 @@ builds items into device cache slots and correlates pairs of resident items
 from __future__ import annotations
 
 import collections
+import dataclasses
 import math
 import threading
 import time
@@ -165,7 +166,8 @@ class ServingEngine:
         self.device = torch.device(device if device is not None else "cuda")
         self.budget = Budget(budget_bytes)
         self.max_batch = max_batch
-        self.cfg = cfg or EngineConfig(segments=16)
+        # queries and the database are separate arenas: the pair kernel reads raw keys
+        self.cfg = dataclasses.replace(cfg or EngineConfig(segments=16), compress=False)
         if self.cfg.segments <= 0:
             raise ValueError("serving needs a fixed number of key segments")
         self.nslots = slots

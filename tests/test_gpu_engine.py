@@ -38,11 +38,13 @@ def many():
     return p, arena, oracle_matrix(p)
 
 
-@pytest.mark.parametrize("wshift,fold,rows", [(10, 16, 16), (9, 8, 16), (11, 16, 16),
-                                              (10, 16, 32), (9, 16, 32), (10, 8, 32)])
-def test_allpairs_matches_fp64(small, wshift, fold, rows):
+@pytest.mark.parametrize("wshift,fold,rows,compress", [
+    (10, 16, 16, True), (9, 8, 16, True), (11, 16, 16, True), (10, 16, 16, False),
+    (10, 16, 32, True), (9, 16, 32, True), (10, 8, 32, False)])
+def test_allpairs_matches_fp64(small, wshift, fold, rows, compress):
     p, arena, C_ref = small
-    eng = PairEngine(arena, EngineConfig(wshift=wshift, fold=fold, tile_rows=rows))
+    eng = PairEngine(arena, EngineConfig(wshift=wshift, fold=fold, tile_rows=rows,
+                                         compress=compress))
     eng.ensure_index()
     plan = eng.plan_triangle()
     out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
@@ -95,9 +97,29 @@ def test_rectangle_plan(small):
     assert err.max() <= 1e-6
 
 
-def test_window_index(small):
+def test_key_ranks(small):
     p, arena, _ = small
     eng = PairEngine(arena, EngineConfig(wshift=10))
+    eng.ensure_index()
+    keys = [arena.host_vector(v)[0] for v in range(arena.n)]
+    union = np.unique(np.concatenate(keys))
+    assert arena.rank_limit == len(union)
+    rk = arena.rkeys.cpu().numpy().view(np.uint32)
+    for v in range(arena.n):
+        o, m, end = int(arena.off[v]), int(arena.nnz[v]), int(arena.off[v + 1])
+        assert np.array_equal(rk[o:o + m], np.searchsorted(union, keys[v]))
+        assert np.all(rk[o + m:end] == 0xFFFFFFFF)  # padding kept
+    # the window index is built on the ranks
+    roff = arena.roff.cpu().numpy()
+    for v in (0, 11):
+        r = np.searchsorted(union, keys[v])
+        expect = np.searchsorted(r, np.arange(arena.R + 1, dtype=np.int64) << 10)
+        assert np.array_equal(roff[v, :arena.R + 1], expect)
+
+
+def test_window_index(small):
+    p, arena, _ = small
+    eng = PairEngine(arena, EngineConfig(wshift=10, compress=False))
     eng.ensure_index()
     roff = arena.roff.cpu().numpy()
     for v in (0, 7, 19):
