@@ -104,9 +104,9 @@ long phyloBuildBatchScratch(const char *alphabet, int k, int max_proteomes, long
 /* Phase 1: counting, candidate slots, Markov alpha, norms, per-proteome sizes.
  * d_seq: concatenated residue bytes; d_seq_off: uint64[num_proteomes + 1].
  * h_nnz (host int64[num_proteomes]) receives the vector sizes, h_candidates
- * (host int64, may be 0) the total candidate slots.  Returns
- * cudaErrorMemoryAllocation (2) when the slots exceed max_candidates (retry
- * with *h_candidates).  Synchronous. */
+ * (host int64, may be 0) the candidate slots the batch needs (each proteome's
+ * rounded up to 2048).  Returns cudaErrorMemoryAllocation (2) when they exceed
+ * max_candidates rounded up to 2048 (retry with *h_candidates).  Synchronous. */
 int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
                         const char *alphabet, int k, int num_proteomes, uintptr_t d_seq,
                         uintptr_t d_seq_off, long max_candidates, int64_t *h_nnz,

@@ -269,8 +269,8 @@ int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size
     PHYLO_CHECK(cudaMemcpyAsync(h_nnz, a.nnz, sizeof(uint64_t) * num_proteomes,
                                 cudaMemcpyDeviceToHost, st));
     if (h_candidates)
-        PHYLO_CHECK(cudaMemcpyAsync(h_candidates, a.chunk_cand_off + (uint64_t)num_proteomes * g.NCH,
-                                    sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        PHYLO_CHECK(cudaMemcpyAsync(h_candidates, a.cand_total, sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, st));
     uint32_t status = 0;
     PHYLO_CHECK(last_status(a.status, st, &status));
     if (status & DEV_CAPACITY) {

@@ -18,21 +18,24 @@
 //   k_prep          tile bases per proteome
 //   k_count         (K-2)/(K-1) counts, right-extension masks, window totals
 //   k_cand_count    candidates per chunk of 2048 (K-1)-mers
-//   scan            -> global candidate offsets
-//   k_cand_offsets  per-(K-1)-mer candidate offsets
+//   scan, k_cand_bases   candidate offsets; proteome p's candidates start at
+//                   cbase[p], a multiple of ALPHA_TILE
+//   k_cand_offsets  per-(K-1)-mer candidate offsets; the (K-1)-mer of every candidate
 //   k_c0_zero/k_c0_scatter   K-mer counts into candidate slots
-//   k_alpha         Markov alpha (reference double order), survivor counts,
-//                   exact-ish norm partials (double-double)
-//   scan            -> output offsets
+//   k_alpha         Markov alpha (reference double order) of every candidate, flat
+//                   over the candidates; each warp compacts its segment's survivors
+//                   (alpha bits and key) to the segment's start; norm partials
+//   scan            -> output offset of every segment
 //   k_norm          per-proteome norm, scale, nnz
 //   (host reads nnz, checks capacity)
-//   k_compact       survivors' keys and normalised values, sorted
+//   k_compact       survivors' keys and normalised values, copied segment by segment
 #include "cv_build.cuh"
 #include "scan.cuh"
 
 namespace phylo {
 
-constexpr int TILE = 2048;           // sequence positions per counting tile
+constexpr int TILE = 512;            // sequence positions per counting tile (few
+                                     // proteomes' tables in flight -> L2 hits)
 constexpr int COUNT_THREADS = 256;
 constexpr int CH = 2048;             // (K-1)-mers per chunk
 constexpr int CHUNK_THREADS = 256;
@@ -386,15 +389,35 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     }
     if (q0 < a.T1) *reinterpret_cast<uint4 *>(coff + q0) = make_uint4(o[0], o[1], o[2], o[3]);
     if (q0 + 4 < a.T1) *reinterpret_cast<uint4 *>(coff + q0 + 4) = make_uint4(o[4], o[5], o[6], o[7]);
+    // the (K-1)-mer of every candidate, in the batch's candidate index space
+    const uint64_t gb = a.cbase[p];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint64_t g0 = gb + o[i];
+        for (uint32_t j = 0; j < v[i]; j++)
+            if (g0 + j < a.cand_cap) a.cq[g0 + j] = q0 + (uint32_t)i;
+    }
+}
+
+// cbase[p] = start of proteome p's candidates, rounded up to ALPHA_TILE, so that
+// no k_alpha CTA straddles two proteomes.  One thread.
+__global__ void k_cand_bases(BuildArgs a) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint64_t run = 0;
+    for (int p = 0; p < a.B; p++) {
+        a.cbase[p] = run;
+        const uint64_t n =
+            a.chunk_cand_off[(uint64_t)(p + 1) * a.NCH] - a.chunk_cand_off[(uint64_t)p * a.NCH];
+        run += div_up(n, (uint64_t)ALPHA_TILE) * ALPHA_TILE;
+    }
+    a.cbase[a.B] = run;
+    *a.cand_total = run;
+    if (run > a.cand_cap) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
 }
 
 // zero the K-mer count slots of all candidates (bounded by capacity)
 __global__ void k_c0_zero(BuildArgs a) {
-    uint64_t total = a.chunk_cand_off[(uint64_t)a.B * a.NCH];
-    if (total > a.cand_cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
-        total = a.cand_cap;
-    }
+    const uint64_t total = min(*a.cand_total, a.cand_cap);  // k_cand_bases flags overflow
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (uint64_t)gridDim.x * blockDim.x)
         a.c0a[i] = 0;
@@ -417,7 +440,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
         __syncthreads();
         const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
         const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
-        const uint64_t cbase = a.chunk_cand_off[(uint64_t)p * a.NCH];
+        const uint64_t cbase = a.cbase[p];
         for (int u = 0; u < TILE / COUNT_THREADS; u++) {
             const int li = u * COUNT_THREADS + threadIdx.x;
             bool v0 = false;
@@ -450,38 +473,33 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
     }
 }
 
-// Locate candidate u (chunk-local) -> (K-1)-mer q, symbol b.
-struct ChunkCtx {
-    uint64_t q0;
-    uint32_t nq;
-};
-
-__device__ __forceinline__ void locate(const uint32_t *sm_off, uint32_t nq, uint32_t u,
-                                       uint32_t &ql, uint32_t &r) {
-    // largest ql with sm_off[ql] <= u
-    uint32_t lo = 0, hi = nq;
-    while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (sm_off[mid] <= u) lo = mid; else hi = mid;
-    }
-    ql = lo;
-    r = u - sm_off[lo];
-}
-
-// Markov alpha for every candidate; alpha bits replace the count in place
-// (as native.cu:399 does); per-chunk survivor counts and norm partials.
-// grid = (NCH, B)
+// Markov alpha of every candidate (alpha bits replace the count, as
+// native.cu:399 does), flat over the batch's candidate index space: CTA c takes
+// candidates [c * ALPHA_TILE, (c + 1) * ALPHA_TILE) of one proteome, warp w the
+// segment of SEG candidates starting at c * ALPHA_TILE + w * SEG.  Survivors
+// (alpha bits != 0) are compacted, in key order, to the start of their segment:
+// c0a holds their alpha bits (or TUPLE_TAG | tuple), cq their keys; seg_surv the
+// count.  Per-CTA norm partials.  grid = cand_cap / ALPHA_TILE
 __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
-    __shared__ uint32_t sm_off[CH];
     __shared__ U192 s_norm[CHUNK_THREADS / 32];
-    __shared__ uint32_t s_surv[CHUNK_THREADS / 32], s_m1[CHUNK_THREADS / 32],
-        s_bad[CHUNK_THREADS / 32];
-    const int p = blockIdx.y, c = blockIdx.x;
-    const uint64_t pc = (uint64_t)p * a.NCH + c;
-    const uint64_t cb = a.chunk_cand_off[pc];
-    const uint32_t ncand = (uint32_t)(a.chunk_cand_off[pc + 1] - cb);
-    const uint64_t q0 = (uint64_t)c * CH;
-    const uint32_t nq = (uint32_t)min((uint64_t)CH, a.T1 - q0);
+    __shared__ uint32_t s_m1[CHUNK_THREADS / 32], s_bad[CHUNK_THREADS / 32];
+    const uint64_t c = blockIdx.x;
+    const uint64_t g0 = c * ALPHA_TILE;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t seg = c * (ALPHA_TILE / SEG) + w;
+    const uint64_t total = min(*a.cand_total, a.cand_cap);
+    if (g0 >= total) {  // past the last proteome
+        if (lane == 0) a.seg_surv[seg] = 0;
+        if (threadIdx.x == 0) {
+            a.cta_m1[c] = 0;
+            a.cta_bad[c] = 0;
+            a.cta_norm[3 * c] = a.cta_norm[3 * c + 1] = a.cta_norm[3 * c + 2] = 0;
+        }
+        return;
+    }
+    const int p = find_owner(a.cbase, a.B, g0);
+    const uint32_t np =
+        (uint32_t)(a.chunk_cand_off[(uint64_t)(p + 1) * a.NCH] - a.chunk_cand_off[(uint64_t)p * a.NCH]);
     const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
     const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
     const uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
@@ -489,47 +507,53 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     const double *prob = a.prob + (uint64_t)p * 4 * PROB_TABLE;
     const uint32_t *atab = a.atab + (uint64_t)p * TUPLE_TABLE;
     const uint32_t n0 = a.tot[p * 4 + 0], n1 = a.tot[p * 4 + 1], n2 = a.tot[p * 4 + 2];
-    uint32_t local0 = ncand ? coff[q0] : 0;
-    for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
-    __syncthreads();
-    U192 acc = {0, 0, 0};
-    uint32_t surv = 0, m1 = 0, bad = 0;
     const uint32_t A = a.A;
-    for (uint32_t u = threadIdx.x; u < ncand; u += CHUNK_THREADS) {
-        if (cb + u >= a.cand_cap) break;
-        uint32_t ql, r;
-        locate(sm_off, nq, u, ql, r);
-        const uint32_t q = (uint32_t)(q0 + ql);
-        const uint32_t m = a.fdT2.mod(q);
-        const uint32_t b = nth_set_bit(mk[m], r);
-        const uint32_t full = a.c0a[cb + u];
-        const uint32_t pre = c1[q];
-        const uint32_t suf = c1[m * A + b];
-        const uint32_t mid = c2[m];
-        float f;
-        uint32_t stored;
-        if (full - 1u < 3u && pre < (uint32_t)TUPLE_PS && suf < (uint32_t)TUPLE_PS &&
-            mid < (uint32_t)TUPLE_MID && n0 != 0u) {
-            const uint32_t t = ((full * TUPLE_PS + pre) * TUPLE_PS + suf) * TUPLE_MID + mid;
-            const uint32_t tb = __ldg(&atab[t]);
-            f = __uint_as_float(tb);
-            stored = tb ? (TUPLE_TAG | t) : 0u;
-        } else {
-            f = markov_alpha_fast(full, pre, suf, mid, n0, n1, n2, prob);
-            stored = __float_as_uint(f);
+    const uint64_t sbase = g0 + (uint64_t)w * SEG;           // this warp's segment
+    const uint32_t loc0 = (uint32_t)(sbase - a.cbase[p]);    // proteome-local index of its start
+    U192 acc = {0, 0, 0};
+    uint32_t m1 = 0, bad = 0, nsurv = 0;
+#pragma unroll 2
+    for (uint32_t i = 0; i < SEG; i += 32) {
+        const uint32_t ul = loc0 + i + lane;
+        const uint64_t u = sbase + i + lane;
+        uint32_t stored = 0, key = 0;
+        float f = 0.0f;
+        if (ul < np) {
+            const uint32_t q = a.cq[u];
+            const uint32_t full = a.c0a[u];
+            const uint32_t m = a.fdT2.mod(q);
+            const uint32_t b = nth_set_bit(__ldg(&mk[m]), ul - __ldg(&coff[q]));
+            const uint32_t pre = __ldg(&c1[q]);
+            const uint32_t suf = __ldg(&c1[m * A + b]);
+            const uint32_t mid = __ldg(&c2[m]);
+            if (full - 1u < 3u && pre < (uint32_t)TUPLE_PS && suf < (uint32_t)TUPLE_PS &&
+                mid < (uint32_t)TUPLE_MID && n0 != 0u) {
+                const uint32_t t = ((full * TUPLE_PS + pre) * TUPLE_PS + suf) * TUPLE_MID + mid;
+                const uint32_t tb = __ldg(&atab[t]);
+                f = __uint_as_float(tb);
+                stored = tb ? (TUPLE_TAG | t) : 0u;
+            } else {
+                f = markov_alpha_fast(full, pre, suf, mid, n0, n1, n2, prob);
+                stored = __float_as_uint(f);
+            }
+            key = q * A + b;
         }
-        const uint32_t bits = __float_as_uint(f);
-        a.c0a[cb + u] = stored;
-        if (bits != 0u) {
-            surv++;
+        const bool surv = __float_as_uint(f) != 0u;
+        const unsigned bal = __ballot_sync(0xffffffffu, surv);
+        if (surv) {
+            // positions at or before this lane's own: already read by this warp
+            const uint64_t pos = sbase + nsurv + __popc(bal & ((1u << lane) - 1u));
+            a.c0a[pos] = stored;
+            a.cq[pos] = key;
             const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
             if (sq == 1.0f) m1++;
             else if (isnan(sq)) bad |= 1u;
             else if (isinf(sq) || !u192_add_float(acc, sq)) bad |= 2u;
         }
+        nsurv += __popc(bal);
     }
-    // reduce (integer: exact and order independent)
-    surv = __reduce_add_sync(0xffffffffu, surv);
+    if (lane == 0) a.seg_surv[seg] = nsurv;
+    // norm partials (integer: exact and order independent)
     m1 = __reduce_add_sync(0xffffffffu, m1);
     bad = __reduce_or_sync(0xffffffffu, bad);
 #pragma unroll
@@ -537,43 +561,42 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
         const U192 o = u192_shfl_down(acc, d);
         u192_add(acc, o.w0, o.w1, o.w2);
     }
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        s_norm[w] = acc; s_surv[w] = surv; s_m1[w] = m1; s_bad[w] = bad;
+    if (lane == 0) {
+        s_norm[w] = acc; s_m1[w] = m1; s_bad[w] = bad;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         U192 t = {0, 0, 0};
-        uint32_t ts = 0, tm = 0, tb = 0;
+        uint32_t tm = 0, tb = 0;
         for (int i = 0; i < CHUNK_THREADS / 32; i++) {
             u192_add(t, s_norm[i].w0, s_norm[i].w1, s_norm[i].w2);
-            ts += s_surv[i];
             tm += s_m1[i];
             tb |= s_bad[i];
         }
-        a.chunk_surv[pc] = ts;
-        a.chunk_m1[pc] = tm;
-        a.chunk_bad[pc] = tb;
-        a.chunk_norm[3 * pc + 0] = t.w0;
-        a.chunk_norm[3 * pc + 1] = t.w1;
-        a.chunk_norm[3 * pc + 2] = t.w2;
+        a.cta_m1[c] = tm;
+        a.cta_bad[c] = tb;
+        a.cta_norm[3 * c + 0] = t.w0;
+        a.cta_norm[3 * c + 1] = t.w1;
+        a.cta_norm[3 * c + 2] = t.w2;
     }
 }
 
 // Per proteome: norm = exact sum of the squares rounded once to double
 // (native.cu:415-428 sums the same float squares in double, in CUB's order),
-// scale = sqrt(norm), its reciprocal, nnz.  grid = B, 32 threads.
+// scale = sqrt(norm), its reciprocal, nnz, output base.  grid = B, 32 threads.
 __global__ void k_norm(BuildArgs a) {
     const int p = blockIdx.x;
     const int lane = threadIdx.x;
+    const uint64_t ncta = a.cand_cap / ALPHA_TILE, nseg = a.cand_cap / SEG;
+    const uint64_t c0 = min(a.cbase[p] / ALPHA_TILE, ncta);
+    const uint64_t c1 = min(a.cbase[p + 1] / ALPHA_TILE, ncta);
     U192 acc = {0, 0, 0};
     uint64_t m1 = 0;
     uint32_t bad = 0;
-    for (uint64_t c = lane; c < a.NCH; c += 32) {
-        const uint64_t pc = (uint64_t)p * a.NCH + c;
-        u192_add(acc, a.chunk_norm[3 * pc], a.chunk_norm[3 * pc + 1], a.chunk_norm[3 * pc + 2]);
-        m1 += a.chunk_m1[pc];
-        bad |= a.chunk_bad[pc];
+    for (uint64_t c = c0 + lane; c < c1; c += 32) {
+        u192_add(acc, a.cta_norm[3 * c], a.cta_norm[3 * c + 1], a.cta_norm[3 * c + 2]);
+        m1 += a.cta_m1[c];
+        bad |= a.cta_bad[c];
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -592,77 +615,51 @@ __global__ void k_norm(BuildArgs a) {
         a.norm[p] = norm;
         a.scale[p] = scale;
         a.rscale[p] = __ddiv_rn(1.0, scale);
-        const uint64_t o0 = a.chunk_out_off[(uint64_t)p * a.NCH];
-        const uint64_t o1 = a.chunk_out_off[(uint64_t)(p + 1) * a.NCH];
+        const uint64_t o0 = a.seg_out_off[min(a.cbase[p] / SEG, nseg)];
+        const uint64_t o1 = a.seg_out_off[min(a.cbase[p + 1] / SEG, nseg)];
         a.nnz[p] = o1 - o0;
         a.out_base[p] = o0;
     }
 }
 
-// Writes survivors in candidate (= key) order: keys and float(alpha / scale)
+// Copies every segment's survivors to the output: keys and float(alpha / scale)
 // (native.cu:460-468).  The division by the per-proteome constant scale uses
 // its correctly rounded reciprocal and one FMA correction (Markstein), which
-// yields the correctly rounded double quotient.  grid = (NCH, B)
+// yields the correctly rounded double quotient.  grid = cand_cap / ALPHA_TILE
 __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
-    __shared__ uint32_t sm_off[CH];
-    __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
-    const int p = blockIdx.y, c = blockIdx.x;
-    const uint64_t pc = (uint64_t)p * a.NCH + c;
-    const uint64_t cb = a.chunk_cand_off[pc];
-    const uint32_t ncand = (uint32_t)(a.chunk_cand_off[pc + 1] - cb);
-    if (a.chunk_surv[pc] == 0) return;
-    const uint64_t q0 = (uint64_t)c * CH;
-    const uint32_t nq = (uint32_t)min((uint64_t)CH, a.T1 - q0);
-    const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
-    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
-    uint32_t local0 = coff[q0];
-    for (uint32_t i = threadIdx.x; i < nq; i += CHUNK_THREADS) sm_off[i] = coff[q0 + i] - local0;
-    __syncthreads();
+    const uint64_t c = blockIdx.x, g0 = c * ALPHA_TILE;
+    if (g0 >= min(*a.cand_total, a.cand_cap)) return;
+    const int p = find_owner(a.cbase, a.B, g0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t seg = c * (ALPHA_TILE / SEG) + w;
+    const uint32_t n = a.seg_surv[seg];
+    if (n == 0) return;
+    const uint64_t src = seg * SEG;
+    const uint64_t dst = a.dst_base[p] + (a.seg_out_off[seg] - a.out_base[p]);
+    const uint64_t dst_end = a.dst_base[p] + a.dst_cap[p];
     const double scale = a.scale[p];
     const double rs = a.rscale[p];
     const float *vtab = a.vtab + (uint64_t)p * TUPLE_TABLE;
     const bool finite = isfinite(scale) && scale > 0.0;
     const float vm1 = __double2float_rn(-rs);  // RN(-1/scale) == -RN(1/scale)
-    // destination: proteome base in the caller's arena + offset within proteome
-    const uint64_t pbase = a.chunk_out_off[(uint64_t)p * a.NCH];
-    uint64_t dst = a.dst_base[p] + (a.chunk_out_off[pc] - pbase);
-    const uint64_t dst_end = a.dst_base[p] + a.dst_cap[p];
-    const uint32_t A = a.A;
-    for (uint32_t base = 0; base < ncand; base += CHUNK_THREADS) {
-        const uint32_t u = base + threadIdx.x;
-        uint32_t bits = 0;
-        uint32_t key = 0;
-        if (u < ncand && cb + u < a.cand_cap) {
-            bits = a.c0a[cb + u];
-            if (bits) {
-                uint32_t ql, r;
-                locate(sm_off, nq, u, ql, r);
-                const uint32_t q = (uint32_t)(q0 + ql);
-                const uint32_t m = a.fdT2.mod(q);
-                key = q * A + nth_set_bit(mk[m], r);
-            }
+    for (uint32_t i = lane; i < n; i += 32) {
+        const uint32_t bits = a.c0a[src + i];
+        const uint32_t key = a.cq[src + i];
+        const float f = __uint_as_float(bits);
+        float v;
+        if ((bits & TUPLE_TAG) == TUPLE_TAG) {
+            v = __ldg(&vtab[bits & ~TUPLE_TAG]);
+        } else if (!finite || !isfinite(f)) {
+            v = __double2float_rn(__ddiv_rn((double)f, scale));
+        } else if (f == -1.0f) {
+            v = vm1;
+        } else {
+            v = div_by_scale(f, scale, rs);
         }
-        uint64_t tot;
-        uint64_t rank = block_excl_scan_u64<CHUNK_THREADS>(bits ? 1u : 0u, sw, &tot);
-        if (bits) {
-            const uint64_t o = dst + rank;
-            if (o < dst_end) {
-                const float f = __uint_as_float(bits);
-                float v;
-                if ((bits & TUPLE_TAG) == TUPLE_TAG) {
-                    v = __ldg(&vtab[bits & ~TUPLE_TAG]);
-                } else if (!finite || !isfinite(f)) {
-                    v = __double2float_rn(__ddiv_rn((double)f, scale));
-                } else if (f == -1.0f) {
-                    v = vm1;
-                } else {
-                    v = div_by_scale(f, scale, rs);
-                }
-                a.out_keys[o] = key;
-                a.out_vals[o] = v;
-            }
+        if (dst + i < dst_end) {
+            a.out_keys[dst + i] = key;
+            a.out_vals[dst + i] = v;
         }
-        dst += tot;
     }
 }
 
@@ -685,8 +682,15 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     return 0;
 }
 
+// Candidate capacity rounded up to whole k_alpha CTAs.
+static uint64_t cand_cap_rounded(uint64_t cand_cap) {
+    return div_up(cand_cap ? cand_cap : 1, (uint64_t)ALPHA_TILE) * ALPHA_TILE;
+}
+
 size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     const uint64_t nc = (uint64_t)B * g.NCH;
+    const uint64_t cap = cand_cap_rounded(cand_cap);
+    const uint64_t ncta = cap / ALPHA_TILE, nseg = cap / SEG;
     size_t s = 0;
     s += scratch_bytes<uint32_t>(g.T1s * B);       // c1 (rows padded to 8 entries)
     s += scratch_bytes<uint32_t>(g.T1s * B);       // coff
@@ -697,15 +701,17 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     s += scratch_bytes<uint64_t>(B + 1);           // tile_base
     s += scratch_bytes<uint32_t>(nc);              // chunk_cand
     s += scratch_bytes<uint64_t>(nc + 1);          // chunk_cand_off
-    s += scratch_bytes<uint32_t>(nc);              // chunk_surv
-    s += scratch_bytes<uint64_t>(nc + 1);          // chunk_out_off
-    s += scratch_bytes<uint32_t>(nc);              // chunk_m1
-    s += scratch_bytes<uint64_t>(3 * nc);          // chunk_norm
-    s += scratch_bytes<uint32_t>(nc);              // chunk_bad
+    s += scratch_bytes<uint64_t>(B + 1);           // cbase
+    s += scratch_bytes<uint64_t>(1);               // cand_total
+    s += scratch_bytes<uint32_t>(nseg);            // seg_surv
+    s += scratch_bytes<uint64_t>(nseg + 1);        // seg_out_off
+    s += scratch_bytes<uint32_t>(ncta);            // cta_m1
+    s += scratch_bytes<uint64_t>(3 * ncta);        // cta_norm
+    s += scratch_bytes<uint32_t>(ncta);            // cta_bad
     s += scratch_bytes<double>(4 * (uint64_t)PROB_TABLE * B);  // prob tables
     s += scratch_bytes<uint32_t>((uint64_t)TUPLE_TABLE * B);   // atab
     s += scratch_bytes<float>((uint64_t)TUPLE_TABLE * B);      // vtab
-    s += scratch_bytes<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);  // scan temp
+    s += scratch_bytes<uint64_t>(scan_temp_bytes(max(nc, nseg) + 1) / 8 + 1);  // scan temp
     s += scratch_bytes<double>(B);                 // norm
     s += scratch_bytes<double>(B);                 // scale
     s += scratch_bytes<double>(B);                 // rscale
@@ -714,7 +720,8 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     s += scratch_bytes<uint64_t>(B);               // dst_base
     s += scratch_bytes<uint64_t>(B);               // dst_cap
     s += scratch_bytes<uint32_t>(4);               // status
-    s += scratch_bytes<uint32_t>(cand_cap);        // c0a
+    s += scratch_bytes<uint32_t>(cap);             // c0a
+    s += scratch_bytes<uint32_t>(cap);             // cq
     return s;
 }
 
@@ -722,6 +729,8 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
                         size_t scratch_size, BuildArgs *a) {
     Scratch sc(scratch, scratch_size);
     const uint64_t nc = (uint64_t)B * g.NCH;
+    const uint64_t cap = cand_cap_rounded(cand_cap);
+    const uint64_t ncta = cap / ALPHA_TILE, nseg = cap / SEG;
     BuildArgs &r = *a;
     r.alpha = g.alpha; r.k = g.k; r.A = g.A; r.T1 = g.T1; r.T2 = g.T2; r.NCH = g.NCH; r.B = B;
     r.T1s = g.T1s;
@@ -734,16 +743,18 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.tile_base = sc.take<uint64_t>(B + 1);
     r.chunk_cand = sc.take<uint32_t>(nc);
     r.chunk_cand_off = sc.take<uint64_t>(nc + 1);
-    r.chunk_surv = sc.take<uint32_t>(nc);
-    r.chunk_out_off = sc.take<uint64_t>(nc + 1);
-    r.chunk_m1 = sc.take<uint32_t>(nc);
-    r.chunk_norm = sc.take<uint64_t>(3 * nc);
-    r.chunk_bad = sc.take<uint32_t>(nc);
+    r.cbase = sc.take<uint64_t>(B + 1);
+    r.cand_total = sc.take<uint64_t>(1);
+    r.seg_surv = sc.take<uint32_t>(nseg);
+    r.seg_out_off = sc.take<uint64_t>(nseg + 1);
+    r.cta_m1 = sc.take<uint32_t>(ncta);
+    r.cta_norm = sc.take<uint64_t>(3 * ncta);
+    r.cta_bad = sc.take<uint32_t>(ncta);
     r.prob = sc.take<double>(4 * (uint64_t)PROB_TABLE * B);
     r.atab = sc.take<uint32_t>((uint64_t)TUPLE_TABLE * B);
     r.vtab = sc.take<float>((uint64_t)TUPLE_TABLE * B);
     r.fdT2.set((uint32_t)g.T2);
-    r.scan_tmp = sc.take<uint64_t>(scan_temp_bytes(nc + 1) / 8 + 1);
+    r.scan_tmp = sc.take<uint64_t>(scan_temp_bytes(max(nc, nseg) + 1) / 8 + 1);
     r.norm = sc.take<double>(B);
     r.scale = sc.take<double>(B);
     r.rscale = sc.take<double>(B);
@@ -752,9 +763,10 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.dst_base = sc.take<uint64_t>(B);
     r.dst_cap = sc.take<uint64_t>(B);
     r.status = sc.take<uint32_t>(4);
-    r.c0a = sc.take<uint32_t>(cand_cap);
-    r.cand_cap = cand_cap;
-    if (!r.c0a) return cudaErrorInvalidValue;  // scratch too small
+    r.c0a = sc.take<uint32_t>(cap);
+    r.cq = sc.take<uint32_t>(cap);
+    r.cand_cap = cap;
+    if (!r.cq) return cudaErrorInvalidValue;  // scratch too small
     return cudaSuccess;
 }
 
@@ -786,11 +798,13 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     dim3 gch((unsigned)a.NCH, (unsigned)a.B);
     k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
+    k_cand_bases<<<1, 32, 0, st>>>(a);
     k_cand_offsets<<<gch, CHUNK_THREADS, 0, st>>>(a);
     k_c0_zero<<<sm_count() * 4, 256, 0, st>>>(a);
     k_c0_scatter<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
-    k_alpha<<<gch, CHUNK_THREADS, 0, st>>>(a);
-    PHYLO_CHECK(scan_u32_to_u64(a.chunk_surv, nc, a.chunk_out_off, a.scan_tmp, st));
+    const unsigned ncta = (unsigned)(a.cand_cap / ALPHA_TILE);
+    k_alpha<<<ncta, CHUNK_THREADS, 0, st>>>(a);
+    PHYLO_CHECK(scan_u32_to_u64(a.seg_surv, a.cand_cap / SEG, a.seg_out_off, a.scan_tmp, st));
     k_norm<<<a.B, 32, 0, st>>>(a);
     k_tuple_value<<<dim3(TUPLE_TABLE / 256, a.B), 256, 0, st>>>(a);
     return cudaGetLastError();
@@ -798,16 +812,15 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
 
 // Phase 2: write survivors to out_keys/out_vals at dst_base[p] (capacity dst_cap[p]).
 cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
-    dim3 gch((unsigned)a.NCH, (unsigned)a.B);
-    k_compact<<<gch, CHUNK_THREADS, 0, st>>>(a);
+    k_compact<<<(unsigned)(a.cand_cap / ALPHA_TILE), CHUNK_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 // Kernel counting per launch of build_plan + build_emit (for launch accounting).
 // Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_tables,
-// k_tuple_alpha, k_cand_count, scan (3), k_cand_offsets, k_c0_zero,
+// k_tuple_alpha, k_cand_count, scan (3), k_cand_bases, k_cand_offsets, k_c0_zero,
 // k_c0_scatter, k_alpha, scan (3), k_norm, k_tuple_value; emit
 // k_arena_offsets, k_compact, k_arena_pad.  (Five memsets are not counted.)
-int build_launches_per_batch() { return 17 + 3; }
+int build_launches_per_batch() { return 18 + 3; }
 
 }  // namespace phylo

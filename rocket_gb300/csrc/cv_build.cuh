@@ -25,6 +25,11 @@ struct FastDiv {
     __device__ __forceinline__ uint32_t mod(uint32_t q) const { return q - div(q) * d; }
 };
 
+// Candidates per k_alpha CTA (proteomes start on multiples of it) and per
+// warp segment (survivors are compacted to the start of their segment).
+constexpr uint32_t ALPHA_TILE = 2048;
+constexpr uint32_t SEG = 256;
+
 // Count -> probability tables are kept for counts below this bound.
 constexpr int PROB_TABLE = 4096;
 
@@ -51,14 +56,21 @@ struct BuildArgs {
     uint32_t *c1, *coff;      // [B][T1]
     uint32_t *c2, *mask;      // [B][T2]
     uint32_t *tot;            // [B][4]: n0, n1, n2, -
-    // per (proteome, chunk)
+    // per (proteome, chunk of CH (K-1)-mers)
     uint32_t *chunk_cand;     // candidates per chunk
     uint64_t *chunk_cand_off; // exclusive scan (global over the batch), [nc+1]
-    uint32_t *chunk_surv;     // survivors per chunk
-    uint64_t *chunk_out_off;  // exclusive scan, [nc+1]
-    uint32_t *chunk_m1;       // survivors with alpha^2 == 1
-    uint64_t *chunk_norm;     // [nc][3]: sum of the other alpha^2 as 192-bit fixed point, 2^-96 units
-    uint32_t *chunk_bad;      // [nc]: bit 0 a NaN square, bit 1 an infinite one
+    // candidate index space: proteome p owns [cbase[p], cbase[p+1]), cbase[p] a
+    // multiple of ALPHA_TILE; cbase[B] = *cand_total
+    uint64_t *cbase;          // [B+1]
+    uint64_t *cand_total;     // [1]
+    uint32_t *cq;             // [cand_cap]: (K-1)-mer of each candidate, then the key of each survivor
+    // per segment of SEG candidates (survivors compacted to the segment's start)
+    uint32_t *seg_surv;       // [nseg]
+    uint64_t *seg_out_off;    // exclusive scan, [nseg+1]
+    // per CTA of k_alpha (ALPHA_TILE candidates)
+    uint32_t *cta_m1;         // survivors with alpha^2 == 1
+    uint64_t *cta_norm;       // [ncta][3]: sum of the other alpha^2 as 192-bit fixed point, 2^-96 units
+    uint32_t *cta_bad;        // bit 0 a NaN square, bit 1 an infinite one
     double *prob;             // [B][4][PROB_TABLE]: c/n0, c/n1, c/n2, 1/(c/n2)
     uint32_t *atab;           // [B][TUPLE_TABLE]: alpha bits of each count tuple
     float *vtab;              // [B][TUPLE_TABLE]: float(alpha / sqrt(norm)) of each tuple
