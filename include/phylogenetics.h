@@ -198,7 +198,7 @@ long phyloSelfDotPartBytes(int num_vectors, long max_vector_len);
  * pair kernel gives the same products on ranks as on keys, over a denser key
  * space; padding keys 0xFFFFFFFF are kept.  key_limit bounds every key (A^K);
  * d_union_size (uint64, device) receives the union size.  Asynchronous. */
-long phyloKeyRankScratch(long key_limit);
+long phyloKeyRankScratch(long key_limit, int num_vectors);
 int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                   uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
                   uintptr_t d_rank_keys, uintptr_t d_union_size);

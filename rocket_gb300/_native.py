@@ -102,7 +102,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloComparePairAsync.argtypes = [c_ptr, c_ptr, c_long, c_ptr, c_ptr, c_int, c_ptr, c_ptr,
                                         c_int, c_ptr]
     L.phyloComparePairAsync.restype = c_int
-    L.phyloKeyRankScratch.argtypes = [c_long]
+    L.phyloKeyRankScratch.argtypes = [c_long, c_int]
     L.phyloKeyRankScratch.restype = c_long
     L.phyloKeyRanks.argtypes = [c_ptr, c_ptr, c_long, c_long, c_ptr, c_ptr, c_int, c_long, c_ptr,
                                 c_ptr]

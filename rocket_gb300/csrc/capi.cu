@@ -443,16 +443,16 @@ int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int 
     return (int)ap_reduce_launch(r, (cudaStream_t)stream);
 }
 
-long phyloKeyRankScratch(long key_limit) {
-    if (key_limit <= 0 || key_limit > 0xffffffffl) return -1;
-    return (long)rank_scratch_bytes((uint64_t)key_limit);
+long phyloKeyRankScratch(long key_limit, int num_vectors) {
+    if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0) return -1;
+    return (long)rank_scratch_bytes((uint64_t)key_limit, (uint32_t)num_vectors);
 }
 
 int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                   uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
                   uintptr_t d_rank_keys, uintptr_t d_union_size) {
     if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0 ||
-        scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit))
+        scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit, (uint32_t)num_vectors))
         return (int)cudaErrorInvalidValue;
     return (int)key_ranks((const uint32_t *)d_keys, (const uint64_t *)d_vec_off,
                           (uint32_t)num_vectors, (uint64_t)max_vector_len, (uint64_t)key_limit,

@@ -37,8 +37,8 @@ namespace phylo {
 constexpr int TILE = 512;            // sequence positions per counting tile (few
                                      // proteomes' tables in flight -> L2 hits)
 constexpr int COUNT_THREADS = 256;
-constexpr int CH = 2048;             // (K-1)-mers per chunk
 constexpr int CHUNK_THREADS = 256;
+constexpr int CH = CHUNK_THREADS * 32;  // (K-1)-mers per chunk: one bitmap word per thread
 
 // ---------------------------------------------------------------------------
 // helpers
@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
         }
         __syncthreads();
         uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
+        uint32_t *seen = a.seen1 + (uint64_t)p * (a.T1s / 32);
         uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
         uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         uint32_t cnt0 = 0, cnt1 = 0, cnt2 = 0;
@@ -305,7 +306,9 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             act = __ballot_sync(0xffffffffu, v1);
             if (v1) {
                 unsigned peers = __match_any_sync(act, w1);
-                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&c1[w1], __popc(peers));
+                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 &&
+                    atomicAdd(&c1[w1], __popc(peers)) == 0u)
+                    atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));  // first sighting of w1
                 const uint32_t bit = 1u << last;
                 if (!(__ldcg(&mk[w2]) & bit)) atomicOr(&mk[w2], bit);
             }
@@ -325,34 +328,26 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
     }
 }
 
-// Candidate counts of the 8 consecutive (K-1)-mers q0..q0+7 (q0 a multiple of 8).
-// Rows of the (K-1)-mer tables are padded to T1s (a multiple of 8) with zero
-// counts, so 16-byte accesses stay aligned and in the row.
-__device__ __forceinline__ void cand_counts8(const BuildArgs &a, int p, uint32_t q0,
-                                             uint32_t (&v)[8]) {
-    const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
-    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const uint32_t qb = q0 + 4 * h;
-        uint4 c = make_uint4(0, 0, 0, 0);
-        if (qb < a.T1) c = __ldg(reinterpret_cast<const uint4 *>(c1 + qb));
-        const uint32_t cs[4] = {c.x, c.y, c.z, c.w};
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-            v[4 * h + u] = cs[u] ? __popc(__ldg(&mk[a.fdT2.mod(qb + u)])) : 0u;
+// Candidates of the seen (K-1)-mers of one word of the seen bitmap (32
+// consecutive (K-1)-mers): |R(m)| = popc(mask[m]) for each seen q = a.m.
+__device__ __forceinline__ uint32_t word_candidates(const BuildArgs &a, const uint32_t *mk,
+                                                    uint32_t q0, uint32_t bits) {
+    uint32_t s = 0;
+    while (bits) {
+        const uint32_t j = __ffs(bits) - 1;
+        bits &= bits - 1;
+        s += __popc(__ldg(&mk[a.fdT2.mod(q0 + j)]));
     }
+    return s;
 }
 
 // Candidates per chunk of CH (K-1)-mers.  grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     const int p = blockIdx.y, c = blockIdx.x;
-    const uint32_t q0 = (uint32_t)c * CH + threadIdx.x * (CH / CHUNK_THREADS);
-    uint32_t v[8];
-    cand_counts8(a, p, q0, v);
-    uint32_t s = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) s += v[i];
+    const uint64_t nw = a.T1s / 32;
+    const uint64_t wd = (uint64_t)c * CHUNK_THREADS + threadIdx.x;
+    const uint32_t bits = wd < nw ? a.seen1[(uint64_t)p * nw + wd] : 0u;
+    uint32_t s = word_candidates(a, a.mask + (uint64_t)p * a.T2, (uint32_t)(wd * 32), bits);
     s = __reduce_add_sync(0xffffffffu, s);
     __shared__ uint32_t ws[CHUNK_THREADS / 32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -364,38 +359,36 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     }
 }
 
-// coff[p][q] = candidate offset of (K-1)-mer q within proteome p.  grid = (NCH, B)
+// coff[p][q] = candidate offset of seen (K-1)-mer q within proteome p (entries
+// of unseen q are not written); cq = the (K-1)-mer of every candidate.
+// grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
     const int p = blockIdx.y, c = blockIdx.x;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
-    const uint32_t q0 = (uint32_t)c * CH + threadIdx.x * (CH / CHUNK_THREADS);
-    uint32_t v[8];
-    cand_counts8(a, p, q0, v);
-    uint64_t s = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) s += v[i];
+    const uint64_t nw = a.T1s / 32;
+    const uint64_t wd = (uint64_t)c * CHUNK_THREADS + threadIdx.x;
+    const uint32_t q0 = (uint32_t)(wd * 32);
+    const uint32_t bits = wd < nw ? a.seen1[(uint64_t)p * nw + wd] : 0u;
+    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+    const uint32_t s = word_candidates(a, mk, q0, bits);
     uint64_t tot;
-    uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
-    const uint32_t base =
+    const uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
+    uint32_t run =
         (uint32_t)(a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH] + ex);
     uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
-    uint32_t o[8];
-    uint32_t run = base;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        o[i] = run;
-        run += v[i];
-    }
-    if (q0 < a.T1) *reinterpret_cast<uint4 *>(coff + q0) = make_uint4(o[0], o[1], o[2], o[3]);
-    if (q0 + 4 < a.T1) *reinterpret_cast<uint4 *>(coff + q0 + 4) = make_uint4(o[4], o[5], o[6], o[7]);
-    // the (K-1)-mer of every candidate, in the batch's candidate index space
     const uint64_t gb = a.cbase[p];
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const uint64_t g0 = gb + o[i];
-        for (uint32_t j = 0; j < v[i]; j++)
-            if (g0 + j < a.cand_cap) a.cq[g0 + j] = q0 + (uint32_t)i;
+    uint32_t rest = bits;
+    while (rest) {
+        const uint32_t j = __ffs(rest) - 1;
+        rest &= rest - 1;
+        const uint32_t q = q0 + j;
+        const uint32_t n = __popc(__ldg(&mk[a.fdT2.mod(q)]));
+        coff[q] = run;
+        // the (K-1)-mer of every candidate, in the batch's candidate index space
+        for (uint32_t i = 0; i < n; i++)
+            if (gb + run + i < a.cand_cap) a.cq[gb + run + i] = q;
+        run += n;
     }
 }
 
@@ -676,7 +669,7 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     g->k = k;
     g->A = (uint32_t)A;
     g->T1 = ipow64(A, k - 1);
-    g->T1s = (g->T1 + 7) / 8 * 8;
+    g->T1s = (g->T1 + 31) / 32 * 32;  // whole words of the seen bitmap
     g->T2 = ipow64(A, k - 2);
     g->NCH = div_up(g->T1, CH);
     return 0;
@@ -694,6 +687,7 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     size_t s = 0;
     s += scratch_bytes<uint32_t>(g.T1s * B);       // c1 (rows padded to 8 entries)
     s += scratch_bytes<uint32_t>(g.T1s * B);       // coff
+    s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // seen1
     s += scratch_bytes<uint32_t>(g.T2 * B);        // c2
     s += scratch_bytes<uint32_t>(g.T2 * B);        // mask
     s += scratch_bytes<uint32_t>(4 * (uint64_t)B); // tot
@@ -736,6 +730,7 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.T1s = g.T1s;
     r.c1 = sc.take<uint32_t>(g.T1s * B);
     r.coff = sc.take<uint32_t>(g.T1s * B);
+    r.seen1 = sc.take<uint32_t>(g.T1s / 32 * B);
     r.c2 = sc.take<uint32_t>(g.T2 * B);
     r.mask = sc.take<uint32_t>(g.T2 * B);
     r.tot = sc.take<uint32_t>(4 * (uint64_t)B);
@@ -786,6 +781,7 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const uint64_t nc = (uint64_t)a.B * a.NCH;
     // dense tables c1 | coff | c2 | mask | tot are contiguous in scratch: zero what needs it
     PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1s * a.B, st));
+    PHYLO_CHECK(cudaMemsetAsync(a.seen1, 0, sizeof(uint32_t) * (a.T1s / 32) * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.mask, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.tot, 0, sizeof(uint32_t) * 4 * a.B, st));

@@ -8,7 +8,7 @@ struct BuildGeometry {
     int alpha, k;
     uint32_t A;      // alphabet size (21 protein, 4 DNA)
     uint64_t T1, T2; // A^(K-1), A^(K-2)
-    uint64_t T1s;    // per-proteome row length of the (K-1)-mer tables (T1 rounded up to 8)
+    uint64_t T1s;    // per-proteome row length of the (K-1)-mer tables (T1 rounded up to 32)
     uint64_t NCH;    // chunks of (K-1)-mers per proteome
 };
 
@@ -53,7 +53,8 @@ struct BuildArgs {
     uint64_t *seq_off_store;  // scratch home for seq_off of a single proteome
     uint64_t *tile_base;      // [B+1]
     // dense per-proteome tables
-    uint32_t *c1, *coff;      // [B][T1]
+    uint32_t *c1, *coff;      // [B][T1s]; coff written for seen (K-1)-mers only
+    uint32_t *seen1;          // [B][T1s / 32]: bitmap of the seen (K-1)-mers
     uint32_t *c2, *mask;      // [B][T2]
     uint32_t *tot;            // [B][4]: n0, n1, n2, -
     // per (proteome, chunk of CH (K-1)-mers)

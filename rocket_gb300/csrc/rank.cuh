@@ -4,8 +4,9 @@
 
 namespace phylo {
 
-// Scratch for key_ranks over keys below key_limit (bitmap + per-word prefix).
-size_t rank_scratch_bytes(uint64_t key_limit);
+// Scratch for key_ranks of N vectors over keys below key_limit (bitmap,
+// per-word prefix, 2^16-key range index).
+size_t rank_scratch_bytes(uint64_t key_limit, uint32_t N);
 
 // ranks[e] = number of distinct keys of the set below keys[e] (padding keys
 // 0xffffffff stay 0xffffffff); *d_union (device) = union size.  Asynchronous.

@@ -306,7 +306,7 @@ class PairEngine:
 
     def _rank(self, a: Arena, st: int) -> None:
         limit = key_limit(a.alphabet, a.k)
-        nb = int(self.L.phyloKeyRankScratch(limit))
+        nb = int(self.L.phyloKeyRankScratch(limit, a.n))
         if getattr(self, "_rank_scratch", None) is None or self._rank_scratch.numel() < nb:
             self._rank_scratch = torch.empty(nb, dtype=torch.uint8, device=self.device)
         if a.rkeys is None or a.rkeys.numel() < a.keys.numel():
@@ -316,7 +316,7 @@ class PairEngine:
         check(self.L.phyloKeyRanks(st, _p(self._rank_scratch), self._rank_scratch.numel(), limit,
                                    _p(a.keys), _p(a.vec_off), a.n, maxlen, _p(a.rkeys),
                                    _p(union)))
-        self.launches += 6
+        self.launches += 7
         a.rank_limit = int(union.cpu().item())  # synchronises: the window count depends on it
         a.ranked = a.n
         a.indexed = 0  # every vector's ranks may have changed
