@@ -115,11 +115,13 @@ int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size
 /* Phase 2 (same scratch and arguments as the Plan): vector p is written at
  * d_keys/d_values[vec_off[p] ..] with vec_off[p] = arena_base + earlier sizes
  * rounded up to 4 entries; d_vec_off (uint64[num_proteomes + 1]) receives the
- * offsets; padding entries get key 0xffffffff, value 0.  Asynchronous. */
+ * offsets; padding entries get key 0xffffffff, value 0.  d_union_bits, when
+ * not 0, is a key bitmap (phyloKeyRankBitmapBytes bytes) in which every
+ * written key's bit is set, for phyloKeyRanks.  Asynchronous. */
 int phyloBuildBatchEmit(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
                         const char *alphabet, int k, int num_proteomes, long max_candidates,
                         uintptr_t d_keys, uintptr_t d_values, uintptr_t d_vec_off,
-                        long arena_base);
+                        long arena_base, uintptr_t d_union_bits);
 
 /* Norms (sum over entries of float(alpha)^2) of the last Plan, host double[]. */
 int phyloBuildBatchNorms(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
@@ -196,12 +198,16 @@ long phyloSelfDotPartBytes(int num_vectors, long max_vector_len);
  * the batched pair path).  d_rank_keys[e] = number of distinct keys of the
  * num_vectors vectors below d_keys[e] -- a strictly increasing map, so the
  * pair kernel gives the same products on ranks as on keys, over a denser key
- * space; padding keys 0xFFFFFFFF are kept.  key_limit bounds every key (A^K);
- * d_union_size (uint64, device) receives the union size.  Asynchronous. */
-long phyloKeyRankScratch(long key_limit, int num_vectors);
+ * space; padding keys 0xFFFFFFFF are kept.  key_limit bounds every key (A^K).
+ * d_union_bits: the union bitmap of the vectors' keys (bit k of uint32 word
+ * k / 32, phyloKeyRankBitmapBytes bytes), as phyloBuildBatchEmit marks it; 0 to
+ * build it here.  d_union_size (uint64, device) receives the union size.
+ * Asynchronous. */
+long phyloKeyRankScratch(long key_limit);
+long phyloKeyRankBitmapBytes(long key_limit);
 int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                   uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
-                  uintptr_t d_rank_keys, uintptr_t d_union_size);
+                  uintptr_t d_union_bits, uintptr_t d_rank_keys, uintptr_t d_union_size);
 
 /* Scratch bytes of phyloComparePairsMany for num_pairs pairs and at most
  * max_tiles merge tiles (sum over pairs of ceil((nl + nr) / 4096)). */

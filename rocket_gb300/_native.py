@@ -70,7 +70,7 @@ def _declare(L: ctypes.CDLL) -> None:
                                       c_long, c_ptr, c_ptr]
     L.phyloBuildBatchPlan.restype = c_int
     L.phyloBuildBatchEmit.argtypes = [c_ptr, c_ptr, c_long, c_char_p, c_int, c_int, c_long, c_ptr,
-                                      c_ptr, c_ptr, c_long]
+                                      c_ptr, c_ptr, c_long, c_ptr]
     L.phyloBuildBatchEmit.restype = c_int
     L.phyloBuildBatchNorms.argtypes = [c_ptr, c_ptr, c_long, c_char_p, c_int, c_int, c_long, c_ptr]
     L.phyloBuildBatchNorms.restype = c_int
@@ -102,10 +102,12 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloComparePairAsync.argtypes = [c_ptr, c_ptr, c_long, c_ptr, c_ptr, c_int, c_ptr, c_ptr,
                                         c_int, c_ptr]
     L.phyloComparePairAsync.restype = c_int
-    L.phyloKeyRankScratch.argtypes = [c_long, c_int]
+    L.phyloKeyRankScratch.argtypes = [c_long]
     L.phyloKeyRankScratch.restype = c_long
+    L.phyloKeyRankBitmapBytes.argtypes = [c_long]
+    L.phyloKeyRankBitmapBytes.restype = c_long
     L.phyloKeyRanks.argtypes = [c_ptr, c_ptr, c_long, c_long, c_ptr, c_ptr, c_int, c_long, c_ptr,
-                                c_ptr]
+                                c_ptr, c_ptr]
     L.phyloKeyRanks.restype = c_int
     L.phyloComparePairsManyScratch.argtypes = [c_int, c_long]
     L.phyloComparePairsManyScratch.restype = c_long
@@ -120,7 +122,8 @@ EXPORTED = [
     "phyloBuildBatchCounts", "phyloBuildLaunchesPerBatch", "phyloWindowIndex",
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsThreads", "phyloPairsLaunch",
     "phyloPairsReduce",
-    "phyloSelfDot", "phyloSelfDotPartBytes", "phyloKeyRankScratch", "phyloKeyRanks",
+    "phyloSelfDot", "phyloSelfDotPartBytes", "phyloKeyRankScratch", "phyloKeyRankBitmapBytes",
+    "phyloKeyRanks",
     "phyloComparePairsManyScratch",
     "phyloComparePairsMany", "phyloComparePairAsync",
 ]

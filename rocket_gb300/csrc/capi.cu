@@ -287,7 +287,7 @@ int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size
 int phyloBuildBatchEmit(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
                         const char *alphabet, int k, int num_proteomes, long max_candidates,
                         uintptr_t d_keys, uintptr_t d_values, uintptr_t d_vec_off,
-                        long arena_base) {
+                        long arena_base, uintptr_t d_union_bits) {
     const int alpha = parse_alphabet(alphabet);
     BuildGeometry g;
     if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0)
@@ -299,6 +299,7 @@ int phyloBuildBatchEmit(uintptr_t stream, uintptr_t d_scratch, long scratch_size
                             (size_t)scratch_size, &a));
     a.out_keys = (uint32_t *)d_keys;
     a.out_vals = (float *)d_values;
+    a.union_bits = (uint32_t *)d_union_bits;
     uint64_t *vec_off = (uint64_t *)d_vec_off;
     k_arena_offsets<<<1, 1, 0, st>>>(a.nnz, num_proteomes, (uint64_t)arena_base, vec_off,
                                      a.dst_base, a.dst_cap);
@@ -443,21 +444,26 @@ int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int 
     return (int)ap_reduce_launch(r, (cudaStream_t)stream);
 }
 
-long phyloKeyRankScratch(long key_limit, int num_vectors) {
-    if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0) return -1;
-    return (long)rank_scratch_bytes((uint64_t)key_limit, (uint32_t)num_vectors);
+long phyloKeyRankScratch(long key_limit) {
+    if (key_limit <= 0 || key_limit > 0xffffffffl) return -1;
+    return (long)rank_scratch_bytes((uint64_t)key_limit);
+}
+
+long phyloKeyRankBitmapBytes(long key_limit) {
+    if (key_limit <= 0 || key_limit > 0xffffffffl) return -1;
+    return (long)(rank_bitmap_words((uint64_t)key_limit) * sizeof(uint32_t));
 }
 
 int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                   uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
-                  uintptr_t d_rank_keys, uintptr_t d_union_size) {
+                  uintptr_t d_union_bits, uintptr_t d_rank_keys, uintptr_t d_union_size) {
     if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0 ||
-        scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit, (uint32_t)num_vectors))
+        scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit))
         return (int)cudaErrorInvalidValue;
     return (int)key_ranks((const uint32_t *)d_keys, (const uint64_t *)d_vec_off,
                           (uint32_t)num_vectors, (uint64_t)max_vector_len, (uint64_t)key_limit,
-                          (void *)d_scratch, (size_t)scratch_bytes, (uint32_t *)d_rank_keys,
-                          (uint64_t *)d_union_size, (cudaStream_t)stream);
+                          (const uint32_t *)d_union_bits, (void *)d_scratch, (size_t)scratch_bytes,
+                          (uint32_t *)d_rank_keys, (uint64_t *)d_union_size, (cudaStream_t)stream);
 }
 
 int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int num_vectors,

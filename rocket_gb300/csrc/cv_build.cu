@@ -297,20 +297,12 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             }
             const bool v2 = run >= K - 2, v1 = run >= K - 1, v0 = run >= K;
             cnt2 += v2; cnt1 += v1; cnt0 += v0;
-            // (K-2)-mer counts, aggregated over equal keys within the warp
-            unsigned act = __ballot_sync(0xffffffffu, v2);
-            if (v2) {
-                unsigned peers = __match_any_sync(act, w2);
-                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&c2[w2], __popc(peers));
-            }
-            act = __ballot_sync(0xffffffffu, v1);
+            // counts: reduction atomics (equal keys within a warp are rare, so
+            // no aggregation); the first sighting of a (K-1)-mer sets its seen bit
+            if (v2) atomicAdd(&c2[w2], 1u);
             if (v1) {
-                unsigned peers = __match_any_sync(act, w1);
-                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 &&
-                    atomicAdd(&c1[w1], __popc(peers)) == 0u)
-                    atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));  // first sighting of w1
-                const uint32_t bit = 1u << last;
-                if (!(__ldcg(&mk[w2]) & bit)) atomicOr(&mk[w2], bit);
+                if (atomicAdd(&c1[w1], 1u) == 0u) atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                atomicOr(&mk[w2], 1u << last);
             }
         }
         // totals
@@ -360,7 +352,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
 }
 
 // coff[p][q] = candidate offset of seen (K-1)-mer q within proteome p (entries
-// of unseen q are not written); cq = the (K-1)-mer of every candidate.
+// of unseen q are not written); head marks of the (K-1)-mers in cq.
 // grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
@@ -385,9 +377,13 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
         const uint32_t q = q0 + j;
         const uint32_t n = __popc(__ldg(&mk[a.fdT2.mod(q)]));
         coff[q] = run;
-        // the (K-1)-mer of every candidate, in the batch's candidate index space
-        for (uint32_t i = 0; i < n; i++)
-            if (gb + run + i < a.cand_cap) a.cq[gb + run + i] = q;
+        // cq marks the first candidate of q, and the first of a segment that q's
+        // run reaches into (the rest of cq is zero); k_alpha recovers the
+        // (K-1)-mer of each candidate as the running maximum of the marks.
+        const uint64_t g = gb + run;
+        if (g < a.cand_cap) a.cq[g] = q;
+        const uint64_t nb = (g / SEG + 1) * SEG;
+        if (nb < g + n && nb < a.cand_cap) a.cq[nb] = q;
         run += n;
     }
 }
@@ -408,12 +404,14 @@ __global__ void k_cand_bases(BuildArgs a) {
     if (run > a.cand_cap) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
 }
 
-// zero the K-mer count slots of all candidates (bounded by capacity)
+// zero the K-mer count slots and (K-1)-mer marks of all candidates (bounded by capacity)
 __global__ void k_c0_zero(BuildArgs a) {
     const uint64_t total = min(*a.cand_total, a.cand_cap);  // k_cand_bases flags overflow
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (uint64_t)gridDim.x * blockDim.x)
+         i += (uint64_t)gridDim.x * blockDim.x) {
         a.c0a[i] = 0;
+        a.cq[i] = 0;
+    }
 }
 
 // Every K-window adds one to the slot of its candidate (native.cu:244).
@@ -455,12 +453,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
                     }
                 }
             }
-            unsigned act = __ballot_sync(0xffffffffu, v0);
-            if (v0) {
-                unsigned peers = __match_any_sync(act, slot);
-                if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && slot < a.cand_cap)
-                    atomicAdd(&a.c0a[slot], __popc(peers));
-            }
+            if (v0 && slot < a.cand_cap) atomicAdd(&a.c0a[slot], 1u);
         }
         __syncthreads();
     }
@@ -504,15 +497,23 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     const uint64_t sbase = g0 + (uint64_t)w * SEG;           // this warp's segment
     const uint32_t loc0 = (uint32_t)(sbase - a.cbase[p]);    // proteome-local index of its start
     U192 acc = {0, 0, 0};
-    uint32_t m1 = 0, bad = 0, nsurv = 0;
-#pragma unroll 2
+    uint32_t m1 = 0, bad = 0, nsurv = 0, carry = 0;
     for (uint32_t i = 0; i < SEG; i += 32) {
         const uint32_t ul = loc0 + i + lane;
         const uint64_t u = sbase + i + lane;
+        // (K-1)-mer of this candidate: the last mark at or before it (marks
+        // ascend along the candidates; every segment starts with one)
+        uint32_t q = ul < np ? a.cq[u] : 0u;
+        q = max(q, carry);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, q, d);
+            if (lane >= d) q = max(q, t);
+        }
+        carry = __shfl_sync(0xffffffffu, q, 31);
         uint32_t stored = 0, key = 0;
         float f = 0.0f;
         if (ul < np) {
-            const uint32_t q = a.cq[u];
             const uint32_t full = a.c0a[u];
             const uint32_t m = a.fdT2.mod(q);
             const uint32_t b = nth_set_bit(__ldg(&mk[m]), ul - __ldg(&coff[q]));
@@ -652,6 +653,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
         if (dst + i < dst_end) {
             a.out_keys[dst + i] = key;
             a.out_vals[dst + i] = v;
+            if (a.union_bits) atomicOr(&a.union_bits[key >> 5], 1u << (key & 31u));
         }
     }
 }
@@ -795,8 +797,8 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
     k_cand_bases<<<1, 32, 0, st>>>(a);
-    k_cand_offsets<<<gch, CHUNK_THREADS, 0, st>>>(a);
     k_c0_zero<<<sm_count() * 4, 256, 0, st>>>(a);
+    k_cand_offsets<<<gch, CHUNK_THREADS, 0, st>>>(a);
     k_c0_scatter<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
     const unsigned ncta = (unsigned)(a.cand_cap / ALPHA_TILE);
     k_alpha<<<ncta, CHUNK_THREADS, 0, st>>>(a);

@@ -88,6 +88,7 @@ struct BuildArgs {
     // output arena
     uint32_t *out_keys;
     float *out_vals;
+    uint32_t *union_bits;     // optional: bit of every written key set (key-rank bitmap)
 };
 
 // Returns 0, -1 (bad alphabet/k) or -2 (keys would not fit uint32).

@@ -10,47 +10,33 @@
 // and different keys stay different -- the products and their order are those
 // of the raw keys, only the windows are denser.
 //
-//   k_range_index   (shift 16) each vector's position of every 2^16-key range
-//   k_rank_mark     one CTA per key range: the union bitmap of the range built
-//                   with shared-memory atomics, then stored whole
+//   k_rank_mark     union bitmap of the keys (reduction atomics), unless the
+//                   caller passes one (the batched build marks survivors' keys)
 //   k_rank_reduce / k_scan_partials / k_rank_prefix
 //                   exclusive prefix of the bitmap's population per 32-bit word
 //   k_rank_apply    rank = prefix[key / 32] + popc(word & bits below key)
 #include "rank.cuh"
-#include "allpairs.cuh"
 #include "scan.cuh"
 
 namespace phylo {
 
-constexpr uint32_t RK_SLICE = 16384;  // entries per CTA (apply)
+constexpr uint32_t RK_SLICE = 16384;  // entries per CTA (mark / apply)
 constexpr uint32_t RK_THREADS = 256;
-constexpr uint32_t RK_RSHIFT = 16;     // key range of one mark CTA: 2^16 keys
-constexpr uint32_t RK_RWORDS = (1u << RK_RSHIFT) / 32;
 
-// grid = key ranges: the union bitmap of keys [r << 16, (r + 1) << 16) over all
-// N vectors (their sub-lists from the range index), stored word by word.
+// grid = (slices, N)
 __global__ void __launch_bounds__(RK_THREADS) k_rank_mark(const uint32_t *__restrict__ keys,
                                                           const uint64_t *__restrict__ vec_off,
-                                                          const uint32_t *__restrict__ roff,
-                                                          uint32_t N, uint32_t R16, uint64_t nwords,
                                                           uint32_t *bits) {
-    __shared__ uint32_t sm[RK_RWORDS];
-    const uint32_t r = blockIdx.x;
-    for (uint32_t i = threadIdx.x; i < RK_RWORDS; i += RK_THREADS) sm[i] = 0;
-    __syncthreads();
-    for (uint32_t v = 0; v < N; v++) {
-        const uint32_t *ro = roff + (uint64_t)v * (R16 + 1);
-        const uint32_t lo = __ldg(&ro[r]), hi = __ldg(&ro[r + 1]);
-        const uint64_t b = __ldg(&vec_off[v]);
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += RK_THREADS) {
-            const uint32_t key = __ldg(&keys[b + e]);
-            atomicOr(&sm[(key >> 5) & (RK_RWORDS - 1)], 1u << (key & 31u));
-        }
+    const uint32_t v = blockIdx.y;
+    const uint64_t b = vec_off[v];
+    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);
+    const uint32_t e0 = blockIdx.x * RK_SLICE;
+    if (e0 >= n) return;
+    const uint32_t e1 = min(n, e0 + RK_SLICE);
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += RK_THREADS) {
+        const uint32_t key = keys[b + e];
+        if (key != 0xffffffffu) atomicOr(&bits[key >> 5], 1u << (key & 31u));  // padding skipped
     }
-    __syncthreads();
-    const uint64_t w0 = (uint64_t)r * RK_RWORDS;
-    for (uint32_t i = threadIdx.x; i < RK_RWORDS; i += RK_THREADS)
-        if (w0 + i < nwords) bits[w0 + i] = sm[i];
 }
 
 // Population of SCAN_TILE words per CTA -> partials[cta].
@@ -115,43 +101,44 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_apply(const uint32_t *__res
 }
 
 static uint64_t rank_words(uint64_t key_limit) { return div_up(key_limit ? key_limit : 1, 32); }
-static uint32_t rank_ranges(uint64_t key_limit) {
-    return (uint32_t)div_up(key_limit ? key_limit : 1, (uint64_t)1 << RK_RSHIFT);
-}
 
-size_t rank_scratch_bytes(uint64_t key_limit, uint32_t N) {
+size_t rank_bitmap_words(uint64_t key_limit) { return rank_words(key_limit); }
+
+size_t rank_scratch_bytes(uint64_t key_limit) {
     const uint64_t nw = rank_words(key_limit);
     const uint64_t nb = div_up(nw, SCAN_TILE);
     return scratch_bytes<uint32_t>(nw) + scratch_bytes<uint32_t>(nw) +
-           scratch_bytes<uint64_t>(nb + 1) + scratch_bytes<uint64_t>(1) +
-           scratch_bytes<uint32_t>((uint64_t)(N ? N : 1) * (rank_ranges(key_limit) + 1));
+           scratch_bytes<uint64_t>(nb + 1) + scratch_bytes<uint64_t>(1);
 }
 
 cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N, uint64_t max_len,
-                      uint64_t key_limit, void *scratch, size_t scratch_size, uint32_t *ranks,
-                      uint64_t *d_union, cudaStream_t st) {
+                      uint64_t key_limit, const uint32_t *union_bits, void *scratch,
+                      size_t scratch_size, uint32_t *ranks, uint64_t *d_union, cudaStream_t st) {
     const uint64_t nw = rank_words(key_limit);
     const uint64_t nb = div_up(nw, SCAN_TILE);
-    const uint32_t R16 = rank_ranges(key_limit);
     Scratch sc(scratch, scratch_size);
-    uint32_t *bits = sc.take<uint32_t>(nw);
+    uint32_t *own = sc.take<uint32_t>(nw);
     uint32_t *prefix = sc.take<uint32_t>(nw);
     uint64_t *partials = sc.take<uint64_t>(nb + 1);
     uint64_t *total = sc.take<uint64_t>(1);
-    uint32_t *roff16 = sc.take<uint32_t>((uint64_t)(N ? N : 1) * (R16 + 1));
-    if (!roff16) return cudaErrorInvalidValue;
-    PHYLO_CHECK(range_index_launch(keys, vec_off, N, R16, RK_RSHIFT, roff16, st, max_len));
-    k_rank_mark<<<R16, RK_THREADS, 0, st>>>(keys, vec_off, roff16, N, R16, nw, bits);
+    if (!total) return cudaErrorInvalidValue;
+    const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, RK_SLICE);
+    const uint32_t *bits = union_bits;
+    if (!bits) {
+        PHYLO_CHECK(cudaMemsetAsync(own, 0, sizeof(uint32_t) * nw, st));
+        if (N) k_rank_mark<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, own);
+        bits = own;
+    }
     k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials);
     k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
     k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials, prefix, total);
-    const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, RK_SLICE);
     if (N) k_rank_apply<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, bits, prefix, ranks);
     if (d_union) PHYLO_CHECK(cudaMemcpyAsync(d_union, total, sizeof(uint64_t),
                                              cudaMemcpyDeviceToDevice, st));
     return cudaGetLastError();
 }
 
-int key_ranks_launches() { return 7; }  // range index, mark, reduce, scan, prefix, apply, copy
+// launches with a caller's bitmap: reduce, scan, prefix, apply, copy (+ mark without one)
+int key_ranks_launches(bool marked) { return marked ? 5 : 6; }
 
 }  // namespace phylo

@@ -4,16 +4,20 @@
 
 namespace phylo {
 
-// Scratch for key_ranks of N vectors over keys below key_limit (bitmap,
-// per-word prefix, 2^16-key range index).
-size_t rank_scratch_bytes(uint64_t key_limit, uint32_t N);
+// Words of the union bitmap of keys below key_limit (bit k of word k / 32).
+size_t rank_bitmap_words(uint64_t key_limit);
+
+// Scratch for key_ranks over keys below key_limit (bitmap + per-word prefix).
+size_t rank_scratch_bytes(uint64_t key_limit);
 
 // ranks[e] = number of distinct keys of the set below keys[e] (padding keys
-// 0xffffffff stay 0xffffffff); *d_union (device) = union size.  Asynchronous.
+// 0xffffffff stay 0xffffffff); *d_union (device) = union size.  union_bits,
+// when not null, is the union bitmap of the set's keys, already marked (the
+// batched build can mark it); otherwise it is built here.  Asynchronous.
 cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N, uint64_t max_len,
-                      uint64_t key_limit, void *scratch, size_t scratch_size, uint32_t *ranks,
-                      uint64_t *d_union, cudaStream_t st);
+                      uint64_t key_limit, const uint32_t *union_bits, void *scratch,
+                      size_t scratch_size, uint32_t *ranks, uint64_t *d_union, cudaStream_t st);
 
-int key_ranks_launches();
+int key_ranks_launches(bool marked);
 
 }  // namespace phylo

@@ -68,6 +68,8 @@ class Arena:
     R: int = 0
     indexed: int = 0            # vectors covered by roff
     rkeys: Optional[torch.Tensor] = None   # dense key ranks (pair kernel input), or None
+    union_bits: Optional[torch.Tensor] = None  # key bitmap the batched build marks
+    union_n: int = 0            # vectors whose keys are marked in union_bits
     rank_limit: int = 0         # union size of the ranked vectors
     ranked: int = 0             # vectors covered by rkeys (ranks of all of them change together)
     index_on_ranks: bool = False
@@ -96,6 +98,9 @@ class Arena:
         self.norms = np.zeros(0, np.float64)
         self.indexed = 0
         self.ranked = 0
+        if self.union_bits is not None:
+            self.union_bits.zero_()
+        self.union_n = 0
         return self
 
     def vector(self, v: int):
@@ -196,9 +201,17 @@ class BatchBuilder:
                 cap = int(max(need, arena.keys.numel() * 1.5))
                 arena.keys = _grow(arena.keys, cap)
                 arena.values = _grow(arena.values, cap)
+            # mark the union bitmap for dense key ranks while every vector is marked
+            mark = arena.union_n == arena.n
+            if mark and arena.union_bits is None:
+                nb = int(self.L.phyloKeyRankBitmapBytes(key_limit(self.alphabet, self.k)))
+                arena.union_bits = torch.zeros(nb // 4, dtype=torch.int32, device=self.device)
             check(self.L.phyloBuildBatchEmit(
                 st, _p(scr), scr.numel(), self.alphabet.encode(), self.k, B, cand,
-                _p(arena.keys), _p(arena.values), _p(arena.vec_off[arena.n:]), arena.used))
+                _p(arena.keys), _p(arena.values), _p(arena.vec_off[arena.n:]), arena.used,
+                _p(arena.union_bits) if mark else 0))
+            if mark:
+                arena.union_n += B
             arena.nnz = np.concatenate([arena.nnz, nnz])
             arena.norms = np.concatenate([arena.norms, norms])
             new_off = arena.used + np.concatenate([[0], np.cumsum(padded)])
@@ -306,17 +319,18 @@ class PairEngine:
 
     def _rank(self, a: Arena, st: int) -> None:
         limit = key_limit(a.alphabet, a.k)
-        nb = int(self.L.phyloKeyRankScratch(limit, a.n))
+        nb = int(self.L.phyloKeyRankScratch(limit))
         if getattr(self, "_rank_scratch", None) is None or self._rank_scratch.numel() < nb:
             self._rank_scratch = torch.empty(nb, dtype=torch.uint8, device=self.device)
         if a.rkeys is None or a.rkeys.numel() < a.keys.numel():
             a.rkeys = torch.empty(a.keys.numel(), dtype=torch.int32, device=self.device)
         union = torch.zeros(1, dtype=torch.int64, device=self.device)
         maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
+        marked = a.union_bits is not None and a.union_n == a.n
         check(self.L.phyloKeyRanks(st, _p(self._rank_scratch), self._rank_scratch.numel(), limit,
-                                   _p(a.keys), _p(a.vec_off), a.n, maxlen, _p(a.rkeys),
-                                   _p(union)))
-        self.launches += 7
+                                   _p(a.keys), _p(a.vec_off), a.n, maxlen,
+                                   _p(a.union_bits) if marked else 0, _p(a.rkeys), _p(union)))
+        self.launches += 5 if marked else 6
         a.rank_limit = int(union.cpu().item())  # synchronises: the window count depends on it
         a.ranked = a.n
         a.indexed = 0  # every vector's ranks may have changed

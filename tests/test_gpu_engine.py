@@ -115,6 +115,13 @@ def test_key_ranks(small):
         r = np.searchsorted(union, keys[v])
         expect = np.searchsorted(r, np.arange(arena.R + 1, dtype=np.int64) << 10)
         assert np.array_equal(roff[v, :arena.R + 1], expect)
+    # the bitmap the build marked and one marked from the keys give the same ranks
+    assert arena.union_n == arena.n
+    saved = arena.union_n
+    arena.union_n, arena.ranked = -1, 0
+    eng.ensure_index()
+    assert np.array_equal(arena.rkeys.cpu().numpy().view(np.uint32), rk)
+    arena.union_n = saved
 
 
 def test_window_index(small):
