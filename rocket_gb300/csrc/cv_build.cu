@@ -380,6 +380,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
         // cq marks the first candidate of q, and the first of a segment that q's
         // run reaches into (the rest of cq is zero); k_alpha recovers the
         // (K-1)-mer of each candidate as the running maximum of the marks.
+        if (n == 0) continue;  // no candidate: its offset is the next one's
         const uint64_t g = gb + run;
         if (g < a.cand_cap) a.cq[g] = q;
         const uint64_t nb = (g / SEG + 1) * SEG;
