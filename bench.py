@@ -551,7 +551,8 @@ def main():
                     help="pair kernel on raw keys instead of dense key ranks")
     ap.add_argument("--tile-rows", type=int, default=16, choices=[16, 32],
                     help="row vectors per pair-kernel work item (selects the kernel)")
-    ap.add_argument("--fold", type=int, default=16)
+    ap.add_argument("--fold", type=int, default=28,
+                    help="products per FP32 accumulator between compensated folds (multiple of 4)")
     ap.add_argument("--items-per-cta", type=int, default=4)
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--ref-seconds", type=float, default=15.0)

@@ -169,7 +169,10 @@ int phyloPairsThreads(int window_shift, int tile_rows);
  * column vectors from the column arena (pass the same arena twice for the
  * pairs of one set; a query batch against a resident database passes two).
  * d_counter (uint32) must be 0; partial blocks of tile_rows x 64 float pairs go
- * to d_part; d_item_cycles (int64[num_items]) may be 0.  Asynchronous. */
+ * to d_part; d_item_cycles (int64[num_items]) may be 0.  fold: products per
+ * FP32 accumulator between compensated folds, rounded down to a multiple of 4
+ * (<= 0: 28); |error of C| <= (fold + 2) * 2^-24 for unit vectors.
+ * Asynchronous. */
 int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_values,
                      uintptr_t d_row_vec_off, uintptr_t d_row_roff, uintptr_t d_col_keys,
                      uintptr_t d_col_values, uintptr_t d_col_vec_off, uintptr_t d_col_roff,

@@ -419,7 +419,8 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
     a.nitems = (uint32_t)num_items;
     a.counter = (uint32_t *)d_counter;
     a.part = (FF *)d_part;
-    a.fold = fold > 0 ? (uint32_t)fold : 16u;
+    // the 16-row kernel adds four products per accumulator between checks
+    a.fold = fold >= 4 ? (uint32_t)fold & ~3u : (fold > 0 ? 4u : 28u);
     a.item_cycles = (int64_t *)d_item_cycles;
     return (int)ap_launch(a, tile_rows, grid, (cudaStream_t)stream);
 }

@@ -498,54 +498,84 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     const uint64_t sbase = g0 + (uint64_t)w * SEG;           // this warp's segment
     const uint32_t loc0 = (uint32_t)(sbase - a.cbase[p]);    // proteome-local index of its start
     U192 acc = {0, 0, 0};
-    uint32_t m1 = 0, bad = 0, nsurv = 0, carry = 0;
-    for (uint32_t i = 0; i < SEG; i += 32) {
-        const uint32_t ul = loc0 + i + lane;
-        const uint64_t u = sbase + i + lane;
-        // (K-1)-mer of this candidate: the last mark at or before it (marks
-        // ascend along the candidates; every segment starts with one)
-        uint32_t q = ul < np ? a.cq[u] : 0u;
-        q = max(q, carry);
+    uint32_t m1 = 0, bad = 0, nsurv = 0;
+    constexpr int NI = SEG / 32;  // candidates per lane
+    // phase 1: marks and counts of the whole segment, then the (K-1)-mer of
+    // each candidate = the last mark at or before it (marks ascend along the
+    // candidates; every segment starts with one)
+    uint32_t q[NI], full[NI];
+#pragma unroll
+    for (int i = 0; i < NI; i++) {
+        const uint32_t ul = loc0 + 32 * i + lane;
+        const uint64_t u = sbase + 32 * i + lane;
+        q[i] = ul < np ? a.cq[u] : 0u;
+        full[i] = ul < np ? a.c0a[u] : 0u;
+    }
+    uint32_t carry = 0;
+#pragma unroll
+    for (int i = 0; i < NI; i++) {
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, q, d);
-            if (lane >= d) q = max(q, t);
+            const uint32_t t = __shfl_up_sync(0xffffffffu, q[i], d);
+            if (lane >= d) q[i] = max(q[i], t);
         }
-        carry = __shfl_sync(0xffffffffu, q, 31);
-        uint32_t stored = 0, key = 0;
-        float f = 0.0f;
-        if (ul < np) {
-            const uint32_t full = a.c0a[u];
-            const uint32_t m = a.fdT2.mod(q);
-            const uint32_t b = nth_set_bit(__ldg(&mk[m]), ul - __ldg(&coff[q]));
-            const uint32_t pre = __ldg(&c1[q]);
-            const uint32_t suf = __ldg(&c1[m * A + b]);
-            const uint32_t mid = __ldg(&c2[m]);
-            if (full - 1u < 3u && pre < (uint32_t)TUPLE_PS && suf < (uint32_t)TUPLE_PS &&
-                mid < (uint32_t)TUPLE_MID && n0 != 0u) {
-                const uint32_t t = ((full * TUPLE_PS + pre) * TUPLE_PS + suf) * TUPLE_MID + mid;
-                const uint32_t tb = __ldg(&atab[t]);
-                f = __uint_as_float(tb);
-                stored = tb ? (TUPLE_TAG | t) : 0u;
-            } else {
-                f = markov_alpha_fast(full, pre, suf, mid, n0, n1, n2, prob);
-                stored = __float_as_uint(f);
+        q[i] = max(q[i], carry);
+        carry = __shfl_sync(0xffffffffu, q[i], 31);
+    }
+    // phase 2: alpha, four candidates per lane at a time (their table loads in flight together)
+#pragma unroll
+    for (int h = 0; h < NI; h += 4) {
+        uint32_t mm[4], mkv[4], co[4], pre[4], mid[4], b[4], suf[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            mm[j] = a.fdT2.mod(q[h + j]);
+            const bool ok = loc0 + 32 * (h + j) + lane < np;
+            mkv[j] = ok ? __ldg(&mk[mm[j]]) : 0u;
+            co[j] = ok ? __ldg(&coff[q[h + j]]) : 0u;
+            pre[j] = ok ? __ldg(&c1[q[h + j]]) : 0u;
+            mid[j] = ok ? __ldg(&c2[mm[j]]) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t ul = loc0 + 32 * (h + j) + lane;
+            const bool ok = ul < np;
+            b[j] = ok ? nth_set_bit(mkv[j], ul - co[j]) : 0u;
+            suf[j] = ok ? __ldg(&c1[mm[j] * A + b[j]]) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int i = h + j;
+            const bool ok = loc0 + 32 * i + lane < np;
+            uint32_t stored = 0, key = 0;
+            float f = 0.0f;
+            if (ok) {
+                if (full[i] - 1u < 3u && pre[j] < (uint32_t)TUPLE_PS &&
+                    suf[j] < (uint32_t)TUPLE_PS && mid[j] < (uint32_t)TUPLE_MID && n0 != 0u) {
+                    const uint32_t t =
+                        ((full[i] * TUPLE_PS + pre[j]) * TUPLE_PS + suf[j]) * TUPLE_MID + mid[j];
+                    const uint32_t tb = __ldg(&atab[t]);
+                    f = __uint_as_float(tb);
+                    stored = tb ? (TUPLE_TAG | t) : 0u;
+                } else {
+                    f = markov_alpha_fast(full[i], pre[j], suf[j], mid[j], n0, n1, n2, prob);
+                    stored = __float_as_uint(f);
+                }
+                key = q[i] * A + b[j];
             }
-            key = q * A + b;
+            const bool surv = __float_as_uint(f) != 0u;
+            const unsigned bal = __ballot_sync(0xffffffffu, surv);
+            if (surv) {
+                // positions at or before this lane's own: already read (phase 1)
+                const uint64_t pos = sbase + nsurv + __popc(bal & ((1u << lane) - 1u));
+                a.c0a[pos] = stored;
+                a.cq[pos] = key;
+                const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
+                if (sq == 1.0f) m1++;
+                else if (isnan(sq)) bad |= 1u;
+                else if (isinf(sq) || !u192_add_float(acc, sq)) bad |= 2u;
+            }
+            nsurv += __popc(bal);
         }
-        const bool surv = __float_as_uint(f) != 0u;
-        const unsigned bal = __ballot_sync(0xffffffffu, surv);
-        if (surv) {
-            // positions at or before this lane's own: already read by this warp
-            const uint64_t pos = sbase + nsurv + __popc(bal & ((1u << lane) - 1u));
-            a.c0a[pos] = stored;
-            a.cq[pos] = key;
-            const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
-            if (sq == 1.0f) m1++;
-            else if (isnan(sq)) bad |= 1u;
-            else if (isinf(sq) || !u192_add_float(acc, sq)) bad |= 2u;
-        }
-        nsurv += __popc(bal);
     }
     if (lane == 0) a.seg_surv[seg] = nsurv;
     // norm partials (integer: exact and order independent)

@@ -39,7 +39,7 @@ def many():
 
 
 @pytest.mark.parametrize("wshift,fold,rows,compress", [
-    (10, 16, 16, True), (9, 8, 16, True), (11, 16, 16, True), (10, 16, 16, False),
+    (10, 28, 16, True), (9, 8, 16, True), (11, 16, 16, True), (10, 16, 16, False),
     (10, 16, 32, True), (9, 16, 32, True), (10, 8, 32, False)])
 def test_allpairs_matches_fp64(small, wshift, fold, rows, compress):
     p, arena, C_ref = small
