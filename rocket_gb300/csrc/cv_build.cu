@@ -297,11 +297,13 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             }
             const bool v2 = run >= K - 2, v1 = run >= K - 1, v0 = run >= K;
             cnt2 += v2; cnt1 += v1; cnt0 += v0;
-            // counts: reduction atomics (equal keys within a warp are rare, so
-            // no aggregation); the first sighting of a (K-1)-mer sets its seen bit
+            // counts, extension masks and the seen bitmap: reduction atomics only
+            // (no result is waited for; equal keys within a warp are rare, so no
+            // aggregation)
             if (v2) atomicAdd(&c2[w2], 1u);
             if (v1) {
-                if (atomicAdd(&c1[w1], 1u) == 0u) atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                atomicAdd(&c1[w1], 1u);
+                atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
                 atomicOr(&mk[w2], 1u << last);
             }
         }
@@ -340,6 +342,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     const uint64_t wd = (uint64_t)c * CHUNK_THREADS + threadIdx.x;
     const uint32_t bits = wd < nw ? a.seen1[(uint64_t)p * nw + wd] : 0u;
     uint32_t s = word_candidates(a, a.mask + (uint64_t)p * a.T2, (uint32_t)(wd * 32), bits);
+    if (wd < nw) a.word_cand[(uint64_t)p * nw + wd] = s;
     s = __reduce_add_sync(0xffffffffu, s);
     __shared__ uint32_t ws[CHUNK_THREADS / 32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -363,29 +366,38 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     const uint32_t q0 = (uint32_t)(wd * 32);
     const uint32_t bits = wd < nw ? a.seen1[(uint64_t)p * nw + wd] : 0u;
     const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
-    const uint32_t s = word_candidates(a, mk, q0, bits);
+    const uint32_t s = wd < nw ? a.word_cand[(uint64_t)p * nw + wd] : 0u;
     uint64_t tot;
     const uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
     uint32_t run =
         (uint32_t)(a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH] + ex);
     uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
     const uint64_t gb = a.cbase[p];
+    // cq marks (q + 1) the first candidate of q, and the first of a segment that
+    // q's run reaches into (the rest of cq is zero); k_alpha takes each
+    // candidate's (K-1)-mer from the last mark at or before it.  Set bits four
+    // at a time, so that their mask loads are in flight together.
     uint32_t rest = bits;
     while (rest) {
-        const uint32_t j = __ffs(rest) - 1;
-        rest &= rest - 1;
-        const uint32_t q = q0 + j;
-        const uint32_t n = __popc(__ldg(&mk[a.fdT2.mod(q)]));
-        coff[q] = run;
-        // cq marks the first candidate of q, and the first of a segment that q's
-        // run reaches into (the rest of cq is zero); k_alpha recovers the
-        // (K-1)-mer of each candidate as the running maximum of the marks.
-        if (n == 0) continue;  // no candidate: its offset is the next one's
-        const uint64_t g = gb + run;
-        if (g < a.cand_cap) a.cq[g] = q;
-        const uint64_t nb = (g / SEG + 1) * SEG;
-        if (nb < g + n && nb < a.cand_cap) a.cq[nb] = q;
-        run += n;
+        uint32_t qs[4], ns[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            qs[t] = rest ? q0 + (uint32_t)(__ffs(rest) - 1) : 0xffffffffu;
+            rest &= rest - 1;
+            ns[t] = qs[t] != 0xffffffffu ? (uint32_t)__popc(__ldg(&mk[a.fdT2.mod(qs[t])])) : 0u;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            if (qs[t] == 0xffffffffu) break;
+            const uint32_t q = qs[t], n = ns[t];
+            coff[q] = run;
+            if (n == 0) continue;  // no candidate: its offset is the next one's
+            const uint64_t g = gb + run;
+            if (g < a.cand_cap) a.cq[g] = q + 1u;
+            const uint64_t nb = (g / SEG + 1) * SEG;
+            if (nb < g + n && nb < a.cand_cap) a.cq[nb] = q + 1u;
+            run += n;
+        }
     }
 }
 
@@ -512,14 +524,12 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
         full[i] = ul < np ? a.c0a[u] : 0u;
     }
     uint32_t carry = 0;
+    const uint32_t le = 0xffffffffu >> (31 - lane);  // lanes at or below this one
 #pragma unroll
     for (int i = 0; i < NI; i++) {
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, q[i], d);
-            if (lane >= d) q[i] = max(q[i], t);
-        }
-        q[i] = max(q[i], carry);
+        const uint32_t marks = __ballot_sync(0xffffffffu, q[i] != 0u) & le;
+        const uint32_t v = __shfl_sync(0xffffffffu, q[i], marks ? 31 - __clz(marks) : 0);
+        q[i] = marks ? v - 1u : carry;
         carry = __shfl_sync(0xffffffffu, q[i], 31);
     }
     // phase 2: alpha, four candidates per lane at a time (their table loads in flight together)
@@ -530,17 +540,18 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
         for (int j = 0; j < 4; j++) {
             mm[j] = a.fdT2.mod(q[h + j]);
             const bool ok = loc0 + 32 * (h + j) + lane < np;
+            const bool seen = ok && full[h + j] != 0u;  // an unseen K-mer's alpha is -1
             mkv[j] = ok ? __ldg(&mk[mm[j]]) : 0u;
             co[j] = ok ? __ldg(&coff[q[h + j]]) : 0u;
-            pre[j] = ok ? __ldg(&c1[q[h + j]]) : 0u;
-            mid[j] = ok ? __ldg(&c2[mm[j]]) : 0u;
+            pre[j] = seen ? __ldg(&c1[q[h + j]]) : 0u;
+            mid[j] = seen ? __ldg(&c2[mm[j]]) : 0u;
         }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const uint32_t ul = loc0 + 32 * (h + j) + lane;
             const bool ok = ul < np;
             b[j] = ok ? nth_set_bit(mkv[j], ul - co[j]) : 0u;
-            suf[j] = ok ? __ldg(&c1[mm[j] * A + b[j]]) : 0u;
+            suf[j] = ok && full[h + j] != 0u ? __ldg(&c1[mm[j] * A + b[j]]) : 0u;
         }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
@@ -721,6 +732,7 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     s += scratch_bytes<uint32_t>(g.T1s * B);       // c1 (rows padded to 8 entries)
     s += scratch_bytes<uint32_t>(g.T1s * B);       // coff
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // seen1
+    s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // word_cand
     s += scratch_bytes<uint32_t>(g.T2 * B);        // c2
     s += scratch_bytes<uint32_t>(g.T2 * B);        // mask
     s += scratch_bytes<uint32_t>(4 * (uint64_t)B); // tot
@@ -764,6 +776,7 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.c1 = sc.take<uint32_t>(g.T1s * B);
     r.coff = sc.take<uint32_t>(g.T1s * B);
     r.seen1 = sc.take<uint32_t>(g.T1s / 32 * B);
+    r.word_cand = sc.take<uint32_t>(g.T1s / 32 * B);
     r.c2 = sc.take<uint32_t>(g.T2 * B);
     r.mask = sc.take<uint32_t>(g.T2 * B);
     r.tot = sc.take<uint32_t>(4 * (uint64_t)B);

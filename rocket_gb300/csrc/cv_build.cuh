@@ -55,6 +55,7 @@ struct BuildArgs {
     // dense per-proteome tables
     uint32_t *c1, *coff;      // [B][T1s]; coff written for seen (K-1)-mers only
     uint32_t *seen1;          // [B][T1s / 32]: bitmap of the seen (K-1)-mers
+    uint32_t *word_cand;      // [B][T1s / 32]: candidates of each bitmap word
     uint32_t *c2, *mask;      // [B][T2]
     uint32_t *tot;            // [B][4]: n0, n1, n2, -
     // per (proteome, chunk of CH (K-1)-mers)
@@ -64,7 +65,7 @@ struct BuildArgs {
     // multiple of ALPHA_TILE; cbase[B] = *cand_total
     uint64_t *cbase;          // [B+1]
     uint64_t *cand_total;     // [1]
-    uint32_t *cq;             // [cand_cap]: (K-1)-mer of each candidate, then the key of each survivor
+    uint32_t *cq;             // [cand_cap]: (K-1)-mer marks (q + 1), then the key of each survivor
     // per segment of SEG candidates (survivors compacted to the segment's start)
     uint32_t *seg_surv;       // [nseg]
     uint64_t *seg_out_off;    // exclusive scan, [nseg+1]
