@@ -320,7 +320,8 @@ def run_ours(args):
     seq.copy_(pinned)
     builder = BatchBuilder("protein", args.k, device=dev, max_batch=args.max_batch)
     cfg = EngineConfig(wshift=args.wshift, fold=args.fold, items_per_cta=args.items_per_cta,
-                       tile_rows=args.tile_rows, compress=not args.no_compress)
+                       tile_rows=args.tile_rows, tile_cols=args.tile_cols,
+                       compress=not args.no_compress)
     out = torch.zeros((N, N), dtype=torch.float64, device=dev)
     out_host = torch.zeros((N, N), dtype=torch.float64).pin_memory()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -410,6 +411,8 @@ def run_ours(args):
     k_ms = float(np.mean(kernel_ms))
     achieved = alg_bytes / (k_ms / 1000.0) / 1e9
     kernel_name = "k_allpairs32" if args.tile_rows == 32 else "k_allpairs"
+    if args.tile_rows == 16 and args.tile_cols != 64:
+        kernel_name += f"_c{args.tile_cols}"
     traffic = _traffic_per_launch(kernel_name, args.workload, args.wshift)
     line = {
         "metric": "pairwise CV distances/s", "value": value, "unit": "pairs/s",
@@ -421,7 +424,8 @@ def run_ours(args):
             "parallelism": "replicas" if world > 1 else "single GPU",
             "l2": "flushed between steps (512 MB write, outside the timed events)",
             "nnz_mean": float(nnz.mean()), "nnz_total": int(nnz.sum()),
-            "window_shift": args.wshift, "tile_rows": args.tile_rows, "fold": args.fold,
+            "window_shift": args.wshift, "tile_rows": args.tile_rows,
+            "tile_cols": args.tile_cols, "fold": args.fold,
             "key_ranks": not args.no_compress, "windows": int(engine.arena.R),
             "items": plan.nitems,
             "segments": plan.S,
@@ -485,6 +489,7 @@ def run_serve(args):
     srv = ServingEngine("protein", 6, budget_bytes=args.budget_gb * 1e9, slots=args.slots,
                         max_batch=64, cfg=EngineConfig(wshift=args.wshift, fold=args.fold,
                                                        tile_rows=args.tile_rows,
+                                                       tile_cols=args.tile_cols,
                                                        segments=args.segments))
     lens = db.lengths()
     capacity_entries = int(min(np.sum(8 * wl.lengths() + 64),
@@ -551,6 +556,8 @@ def main():
                     help="pair kernel on raw keys instead of dense key ranks")
     ap.add_argument("--tile-rows", type=int, default=16, choices=[16, 32],
                     help="row vectors per pair-kernel work item (selects the kernel)")
+    ap.add_argument("--tile-cols", type=int, default=64, choices=[32, 64],
+                    help="column vectors per pair-kernel work item (32: 128-thread CTAs)")
     ap.add_argument("--fold", type=int, default=28,
                     help="products per FP32 accumulator between compensated folds (multiple of 4)")
     ap.add_argument("--items-per-cta", type=int, default=4)

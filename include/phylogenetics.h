@@ -149,27 +149,29 @@ int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, in
                      int window_shift, unsigned int num_windows, long max_vector_len,
                      uintptr_t d_roff);
 
-/* tile_rows selects the pair kernel: 16 row vectors per work item (80-byte
- * key records, four lanes per column vector, windows up to 2^11 keys) or 32
- * (128-byte swizzled records, eight lanes per column vector, windows up to
- * 2^10 keys).  Partial blocks are tile_rows x 64 float pairs. */
+/* The tile shape (tile_rows x tile_cols row x column vectors per work item)
+ * selects the pair kernel: 16 x 64 (256 threads) or 16 x 32 (128 threads) use
+ * 80-byte key records and four lanes per column vector, windows up to 2^11
+ * keys; 32 x 64 uses 128-byte swizzled records and eight lanes per column
+ * vector, windows up to 2^10 keys.  Partial blocks are tile_rows x tile_cols
+ * float pairs. */
 
 /* Sets the pair kernel's shared-memory limit for this window width and
  * reports how many CTAs fit on one SM. */
-int phyloPairsPrepare(int window_shift, int tile_rows, int *ctas_per_sm);
+int phyloPairsPrepare(int window_shift, int tile_rows, int tile_cols, int *ctas_per_sm);
 
-/* Dynamic shared memory of the pair kernel; -1 for an unknown tile_rows. */
-int phyloPairsSmemBytes(int window_shift, int tile_rows);
+/* Dynamic shared memory of the pair kernel; -1 for an unknown tile shape. */
+int phyloPairsSmemBytes(int window_shift, int tile_rows, int tile_cols);
 
-/* Threads per CTA of the pair kernel; -1 for an unknown tile_rows. */
-int phyloPairsThreads(int window_shift, int tile_rows);
+/* Threads per CTA of the pair kernel; -1 for an unknown tile shape. */
+int phyloPairsThreads(int window_shift, int tile_rows, int tile_cols);
 
 /* Pair kernel over num_items work items (8 uint32 each: row0, nrow, col0,
  * ncol, w0, w1, part, tile).  Row vectors are read from the row arena and
  * column vectors from the column arena (pass the same arena twice for the
  * pairs of one set; a query batch against a resident database passes two).
- * d_counter (uint32) must be 0; partial blocks of tile_rows x 64 float pairs go
- * to d_part; d_item_cycles (int64[num_items]) may be 0.  fold: products per
+ * d_counter (uint32) must be 0; partial blocks of tile_rows x tile_cols float
+ * pairs go to d_part; d_item_cycles (int64[num_items]) may be 0.  fold: products per
  * FP32 accumulator between compensated folds, rounded down to a multiple of 4
  * (<= 0: 28); |error of C| <= (fold + 2) * 2^-24 for unit vectors.
  * Asynchronous. */
@@ -179,14 +181,14 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
                      unsigned int num_windows, int window_shift, uintptr_t d_rowids,
                      uintptr_t d_colids, uintptr_t d_items, int num_items, uintptr_t d_counter,
                      uintptr_t d_part, int fold, uintptr_t d_item_cycles, int tile_rows,
-                     int grid);
+                     int tile_cols, int grid);
 
 /* Sums the partial blocks of each tile (4 uint32: row0, nrow, col0, ncol) into
  * d_out[rowid * ldc + colid] (double); `upper` keeps pairs whose row position
  * is below the column position, `mirror` also writes the transposed entry. */
 int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
-                     int segments, int tile_rows, uintptr_t d_rowids, uintptr_t d_colids,
-                     uintptr_t d_out, long ldc, int upper, int mirror);
+                     int segments, int tile_rows, int tile_cols, uintptr_t d_rowids,
+                     uintptr_t d_colids, uintptr_t d_out, long ldc, int upper, int mirror);
 
 /* d_out[v * ldc + v] = sum of squares of vector v (the diagonal the
  * reference's run includes, phylogenetics_analysis/Main.java:196); d_part is

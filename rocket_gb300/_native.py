@@ -82,18 +82,18 @@ def _declare(L: ctypes.CDLL) -> None:
     # pair engine
     L.phyloWindowIndex.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_int, c_uint, c_long, c_ptr]
     L.phyloWindowIndex.restype = c_int
-    L.phyloPairsPrepare.argtypes = [c_int, c_int, ctypes.POINTER(c_int)]
+    L.phyloPairsPrepare.argtypes = [c_int, c_int, c_int, ctypes.POINTER(c_int)]
     L.phyloPairsPrepare.restype = c_int
-    L.phyloPairsSmemBytes.argtypes = [c_int, c_int]
+    L.phyloPairsSmemBytes.argtypes = [c_int, c_int, c_int]
     L.phyloPairsSmemBytes.restype = c_int
-    L.phyloPairsThreads.argtypes = [c_int, c_int]
+    L.phyloPairsThreads.argtypes = [c_int, c_int, c_int]
     L.phyloPairsThreads.restype = c_int
     L.phyloPairsLaunch.argtypes = [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                    c_uint, c_int, c_ptr, c_ptr, c_ptr, c_int, c_ptr, c_ptr, c_int,
-                                   c_ptr, c_int, c_int]
+                                   c_ptr, c_int, c_int, c_int]
     L.phyloPairsLaunch.restype = c_int
-    L.phyloPairsReduce.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_int, c_int, c_ptr, c_ptr, c_ptr,
-                                   c_long, c_int, c_int]
+    L.phyloPairsReduce.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_int, c_int, c_int, c_ptr, c_ptr,
+                                   c_ptr, c_long, c_int, c_int]
     L.phyloPairsReduce.restype = c_int
     L.phyloSelfDot.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_long, c_ptr, c_ptr, c_long]
     L.phyloSelfDot.restype = c_int

@@ -40,7 +40,7 @@ namespace phylo {
 // constant offsets.  One extra record (index W) stays zero for masked lanes.
 constexpr uint32_t D_STRIDE = 20;  // floats per key record
 
-size_t ap_ring_bytes();
+static size_t ap_ring_bytes(int threads);
 
 // float index of (key idx, row) in D
 __device__ __forceinline__ uint32_t d_slot(uint32_t idx, uint32_t row) {
@@ -95,7 +95,7 @@ __device__ __forceinline__ void cp_async_wait_ring() {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-size_t ap_ring_bytes() { return (size_t)RING * AP_THREADS * 32; }
+static size_t ap_ring_bytes(int threads) { return (size_t)RING * threads * 32; }
 
 __device__ __forceinline__ FF ff_shfl_xor(FF v, int m) {
     FF r;
@@ -104,23 +104,43 @@ __device__ __forceinline__ FF ff_shfl_xor(FF v, int m) {
     return r;
 }
 
+// Shape of a 16-row work item for a CTA of THREADS threads: four lanes per
+// column vector, so THREADS / 4 columns; each warp scatters AP_TI / warps rows,
+// LPR lanes per row.
+template <int THREADS>
+struct ApShape {
+    static constexpr int NW = THREADS / 32;
+    static constexpr int TJ = THREADS / AP_LPC;  // column vectors per item
+    static constexpr int RPW = AP_TI / NW;       // rows a warp scatters
+    static constexpr int LPR = 32 / RPW;         // lanes per scattered row
+    static constexpr int NPF = RPW;              // prefetched entries per lane (NPF * LPR = 32)
+};
+
 // Column side: four lanes per column vector.  Lane q of a column streams the
 // column's 4-entry groups q, q+4, q+8, ... through its cp.async ring, so the four
 // lanes of a column fetch 64 contiguous bytes per load, and keeps its own 16
 // accumulators for the whole item; the four lanes' sums are combined once, at
-// the end of the item.
-__global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
+// the end of the item.  Row side: lane (srow, sj) of a warp scatters entries
+// sj, sj + LPR, ... of row warp * RPW + srow; the first 32 entries of each row's
+// next window are prefetched into registers.
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
+    using S = ApShape<THREADS>;
+    constexpr int TJ = S::TJ, RPW = S::RPW, LPR = S::LPR, NPF = S::NPF;
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t W = 1u << a.wshift, wmask = W - 1u;
     float *D = reinterpret_cast<float *>(smem);                    // (W + 1) x 16
     uint4 *ring_k = reinterpret_cast<uint4 *>(smem + (size_t)(W + 1) * D_STRIDE * 4);
-    float4 *ring_v = reinterpret_cast<float4 *>(ring_k + RING * AP_THREADS);
+    float4 *ring_v = reinterpret_cast<float4 *>(ring_k + RING * THREADS);
     __shared__ uint32_t s_item;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t jcol = threadIdx.x / AP_LPC, q = threadIdx.x % AP_LPC;
+    const uint32_t srow = lane / LPR, sj = lane % LPR;
+    const uint32_t rr = warp * RPW + srow;  // row position this lane scatters
+    const int rsrc = (int)(srow * LPR);     // first lane of this row
     const uint32_t Rs = a.R + 1;
 
-    for (uint32_t i = threadIdx.x; i < (W + 1) * (D_STRIDE / 4); i += AP_THREADS)
+    for (uint32_t i = threadIdx.x; i < (W + 1) * (D_STRIDE / 4); i += THREADS)
         reinterpret_cast<float4 *>(D)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 
     for (;;) {
@@ -147,95 +167,85 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
 #pragma unroll
         for (int k = 0; k < RING; k++) {
             if (fetch < c_end) {
-                cp_async16(&ring_k[slot_fetch * AP_THREADS + threadIdx.x], a.col.keys + cbase + fetch);
-                cp_async16(&ring_v[slot_fetch * AP_THREADS + threadIdx.x], a.col.vals + cbase + fetch);
+                cp_async16(&ring_k[slot_fetch * THREADS + threadIdx.x], a.col.keys + cbase + fetch);
+                cp_async16(&ring_v[slot_fetch * THREADS + threadIdx.x], a.col.vals + cbase + fetch);
             }
             fetch += 4 * AP_LPC;
             slot_fetch = (slot_fetch + 1) & (RING - 1);
             cp_async_commit();
         }
 
-        // ---- this warp's rows (2*warp, 2*warp + 1)
-        uint32_t rv[2];
-        uint64_t rbase[2];
-        bool has_row[2];
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            const uint32_t row = 2 * warp + k;
-            has_row[k] = row < item.nrow;
-            rv[k] = has_row[k] ? a.rowids[item.row0 + row] : 0u;
-            rbase[k] = a.row.vec_off[rv[k]];
-        }
+        // ---- row side: this lane scatters row rr
+        const bool has_row = rr < item.nrow;
+        const uint32_t rv = has_row ? a.rowids[item.row0 + rr] : 0u;
+        const uint64_t rbase = a.row.vec_off[rv];
+        const uint32_t *ro = a.row.roff + (uint64_t)rv * Rs;
         float acc[16], hi[16], lo[16];
 #pragma unroll
         for (int i = 0; i < 16; i++) acc[i] = hi[i] = lo[i] = 0.0f;
         uint32_t nacc = 0;
 
-        // row window offsets: lane-held for 32 windows; first 32 entries of each
-        // row's next window prefetched into registers
-        uint32_t r_lo[2] = {0, 0}, r_hi[2] = {0, 0};
+        // window offsets of LPR windows, held by the row's lanes; the first 32
+        // entries of the row's next window prefetched, NPF per lane
         uint32_t wb = item.w0;
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            if (has_row[k]) {
-                const uint32_t *ro = a.row.roff + (uint64_t)rv[k] * Rs;
-                r_lo[k] = __ldg(&ro[min(item.w0 + lane, a.R)]);
-                r_hi[k] = __ldg(&ro[min(item.w0 + lane + 1, a.R)]);
-            }
+        uint32_t r_lo = 0, r_hi = 0;
+        if (has_row) {
+            r_lo = __ldg(&ro[min(wb + sj, a.R)]);
+            r_hi = __ldg(&ro[min(wb + sj + 1, a.R)]);
         }
-        uint32_t pk[2] = {0xffffffffu, 0xffffffffu};
-        float pv[2] = {0.f, 0.f};
+        uint32_t pk[NPF];
+        float pv[NPF];
+        {
+            const uint32_t lo0 = __shfl_sync(0xffffffffu, r_lo, rsrc);
+            const uint32_t hi0 = __shfl_sync(0xffffffffu, r_hi, rsrc);
 #pragma unroll
-        for (int k = 0; k < 2; k++) {
-            const uint32_t lo_k = __shfl_sync(0xffffffffu, r_lo[k], 0);
-            const uint32_t hi_k = __shfl_sync(0xffffffffu, r_hi[k], 0);
-            if (has_row[k] && lo_k + lane < hi_k) {
-                pk[k] = __ldg(&a.row.keys[rbase[k] + lo_k + lane]);
-                pv[k] = __ldg(&a.row.vals[rbase[k] + lo_k + lane]);
+            for (int t = 0; t < NPF; t++) {
+                const uint32_t e = lo0 + sj + t * LPR;
+                pk[t] = 0xffffffffu;
+                pv[t] = 0.f;
+                if (has_row && e < hi0) {
+                    pk[t] = __ldg(&a.row.keys[rbase + e]);
+                    pv[t] = __ldg(&a.row.vals[rbase + e]);
+                }
             }
         }
 
         for (uint32_t r = item.w0; r < item.w1; r++) {
             const int sl = (int)(r - wb);
-            // densify window r: first 32 entries from registers, the rest loaded
-            uint32_t ck[2];
-            uint32_t lo_k[2], hi_k[2];
+            const uint32_t lo_r = __shfl_sync(0xffffffffu, r_lo, rsrc + sl);
+            const uint32_t hi_r = __shfl_sync(0xffffffffu, r_hi, rsrc + sl);
+            // scatter window r of row rr: first 32 entries from registers, the rest loaded
+            uint32_t ck[NPF];
 #pragma unroll
-            for (int k = 0; k < 2; k++) {
-                lo_k[k] = __shfl_sync(0xffffffffu, r_lo[k], sl);
-                hi_k[k] = __shfl_sync(0xffffffffu, r_hi[k], sl);
-                ck[k] = pk[k];
-                if (has_row[k]) {
-                    const uint32_t row = 2 * warp + k;
-                    if (pk[k] != 0xffffffffu) D[d_slot(pk[k] & wmask, row)] = pv[k];
-                    for (uint32_t e = lo_k[k] + 32 + lane; e < hi_k[k]; e += 32) {
-                        const uint32_t key = __ldg(&a.row.keys[rbase[k] + e]);
-                        D[d_slot(key & wmask, row)] = __ldg(&a.row.vals[rbase[k] + e]);
-                    }
+            for (int t = 0; t < NPF; t++) {
+                ck[t] = pk[t];
+                if (pk[t] != 0xffffffffu) D[d_slot(pk[t] & wmask, rr)] = pv[t];
+            }
+            if (has_row) {
+                for (uint32_t e = lo_r + 32 + sj; e < hi_r; e += LPR) {
+                    const uint32_t key = __ldg(&a.row.keys[rbase + e]);
+                    D[d_slot(key & wmask, rr)] = __ldg(&a.row.vals[rbase + e]);
                 }
             }
-            // prefetch the next window's row offsets / first entries
+            // prefetch the next window's row offsets and first entries
             if (r + 1 < item.w1) {
-                if (r + 1 - wb >= 32u) {
+                if (r + 1 - wb >= (uint32_t)LPR) {
                     wb = r + 1;
-#pragma unroll
-                    for (int k = 0; k < 2; k++) {
-                        if (has_row[k]) {
-                            const uint32_t *ro = a.row.roff + (uint64_t)rv[k] * Rs;
-                            r_lo[k] = __ldg(&ro[min(wb + lane, a.R)]);
-                            r_hi[k] = __ldg(&ro[min(wb + lane + 1, a.R)]);
-                        }
+                    if (has_row) {
+                        r_lo = __ldg(&ro[min(wb + sj, a.R)]);
+                        r_hi = __ldg(&ro[min(wb + sj + 1, a.R)]);
                     }
                 }
                 const int sn = (int)(r + 1 - wb);
+                const uint32_t nlo = __shfl_sync(0xffffffffu, r_lo, rsrc + sn);
+                const uint32_t nhi = __shfl_sync(0xffffffffu, r_hi, rsrc + sn);
 #pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const uint32_t nlo = __shfl_sync(0xffffffffu, r_lo[k], sn);
-                    const uint32_t nhi = __shfl_sync(0xffffffffu, r_hi[k], sn);
-                    pk[k] = 0xffffffffu;
-                    if (has_row[k] && nlo + lane < nhi) {
-                        pk[k] = __ldg(&a.row.keys[rbase[k] + nlo + lane]);
-                        pv[k] = __ldg(&a.row.vals[rbase[k] + nlo + lane]);
+                for (int t = 0; t < NPF; t++) {
+                    const uint32_t e = nlo + sj + t * LPR;
+                    pk[t] = 0xffffffffu;
+                    if (has_row && e < nhi) {
+                        pk[t] = __ldg(&a.row.keys[rbase + e]);
+                        pv[t] = __ldg(&a.row.vals[rbase + e]);
                     }
                 }
             }
@@ -246,8 +256,8 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
             if (has_col) {
                 while (cur < c_hi) {
                     cp_async_wait_ring();
-                    const uint4 kk = ring_k[slot_cur * AP_THREADS + threadIdx.x];
-                    const float4 vv = ring_v[slot_cur * AP_THREADS + threadIdx.x];
+                    const uint4 kk = ring_k[slot_cur * THREADS + threadIdx.x];
+                    const float4 vv = ring_v[slot_cur * THREADS + threadIdx.x];
                     const uint32_t ks[4] = {kk.x, kk.y, kk.z, kk.w};
                     const float vs[4] = {vv.x, vv.y, vv.z, vv.w};
 #pragma unroll
@@ -263,9 +273,9 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
                     }
                     if (cur + 4 > c_hi) break;  // reaches into the next window: keep it
                     if (fetch < c_end) {
-                        cp_async16(&ring_k[slot_fetch * AP_THREADS + threadIdx.x],
+                        cp_async16(&ring_k[slot_fetch * THREADS + threadIdx.x],
                                    a.col.keys + cbase + fetch);
-                        cp_async16(&ring_v[slot_fetch * AP_THREADS + threadIdx.x],
+                        cp_async16(&ring_v[slot_fetch * THREADS + threadIdx.x],
                                    a.col.vals + cbase + fetch);
                     }
                     fetch += 4 * AP_LPC;
@@ -277,29 +287,28 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
             }
             c_lo = c_hi;
             __syncthreads();
-            // clear window r
+            // clear window r of row rr
 #pragma unroll
-            for (int k = 0; k < 2; k++) {
-                if (has_row[k]) {
-                    const uint32_t row = 2 * warp + k;
-                    if (ck[k] != 0xffffffffu) D[d_slot(ck[k] & wmask, row)] = 0.0f;
-                    for (uint32_t e = lo_k[k] + 32 + lane; e < hi_k[k]; e += 32) {
-                        const uint32_t key = __ldg(&a.row.keys[rbase[k] + e]);
-                        D[d_slot(key & wmask, row)] = 0.0f;
-                    }
+            for (int t = 0; t < NPF; t++)
+                if (ck[t] != 0xffffffffu) D[d_slot(ck[t] & wmask, rr)] = 0.0f;
+            if (has_row) {
+                for (uint32_t e = lo_r + 32 + sj; e < hi_r; e += LPR) {
+                    const uint32_t key = __ldg(&a.row.keys[rbase + e]);
+                    D[d_slot(key & wmask, rr)] = 0.0f;
                 }
             }
+            __syncwarp();
         }
         cp_async_wait_all();
         fold16(acc, hi, lo);
         // combine the column's four lanes (fixed order), lane q writes rows q, q+4, ...
-        FF *dst = a.part + (uint64_t)item.part * (AP_TI * AP_TJ);
+        FF *dst = a.part + (uint64_t)item.part * (AP_TI * TJ);
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             FF v = {hi[i], lo[i]};
             v = ff_merge(v, ff_shfl_xor(v, 1));
             v = ff_merge(v, ff_shfl_xor(v, 2));
-            if ((uint32_t)(i & 3) == q) dst[i * AP_TJ + jcol] = v;
+            if ((uint32_t)(i & 3) == q) dst[i * TJ + jcol] = v;
         }
         if (a.item_cycles && threadIdx.x == 0) a.item_cycles[it] = clock64() - t_start;
     }
@@ -321,6 +330,7 @@ __global__ void __launch_bounds__(AP_THREADS, 2) k_allpairs(ApArgs a) {
 // lane accumulates its own rows, so a column needs no cross-lane combine.
 
 constexpr uint32_t R32_REC = 32;  // floats per key record
+constexpr int R32_TJ = 64;        // column vectors per item
 
 __device__ __forceinline__ uint32_t r32_pos(uint32_t slot, uint32_t row) {
     return slot * R32_REC + ((((row >> 2) ^ (slot & 7u)) << 2) | (row & 3u));
@@ -330,11 +340,11 @@ template <int THREADS>
 struct R32Shape {
     static constexpr int NW = THREADS / 32;       // warps
     static constexpr int CPP = NW * 4;            // columns per pass (4 per warp)
-    static constexpr int PASSES = AP_TJ / CPP;    // column passes per window
+    static constexpr int PASSES = R32_TJ / CPP;   // column passes per window
     static constexpr int RPW = 32 / NW;           // rows a warp scatters
     static constexpr int LPR = 32 / RPW;          // lanes per scattered row
     static constexpr int NPF = RPW;               // prefetched entries per lane (NPF * LPR = 32)
-    static_assert(PASSES * CPP == AP_TJ, "columns per item");
+    static_assert(PASSES * CPP == R32_TJ, "columns per item");
 };
 
 template <int THREADS, int MINB>
@@ -530,7 +540,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs32(ApArgs a) {
             __syncwarp();
         }
         // fold and write: lane g of column jc owns rows 4g..4g+3
-        FF *dst = a.part + (uint64_t)item.part * (32 * AP_TJ);
+        FF *dst = a.part + (uint64_t)item.part * (32 * R32_TJ);
 #pragma unroll
         for (int p = 0; p < PASSES; p++) {
             const uint32_t jc = p * S::CPP + warp * 4 + (lane >> 3);
@@ -541,7 +551,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs32(ApArgs a) {
                 two_sum(hi[p][u], acc[p][u], s2, e2);
                 FF v;
                 two_sum(s2, __fadd_rn(lo[p][u], e2), v.hi, v.lo);
-                dst[(4 * g + u) * AP_TJ + jc] = v;
+                dst[(4 * g + u) * R32_TJ + jc] = v;
             }
         }
         if (a.item_cycles && threadIdx.x == 0) a.item_cycles[it] = clock64() - t_start;
@@ -555,44 +565,58 @@ static size_t r32_smem_bytes(uint32_t wshift) {
 }
 static bool r32_wide(uint32_t wshift) { return r32_smem_bytes(wshift) > 100 * 1024; }
 
-size_t ap_smem_bytes(uint32_t wshift, int tile_rows) {
+bool ap_shape_ok(int tile_rows, int tile_cols) {
+    return (tile_rows == 16 && (tile_cols == 64 || tile_cols == 32)) ||
+           (tile_rows == 32 && tile_cols == 64);
+}
+
+size_t ap_smem_bytes(uint32_t wshift, int tile_rows, int tile_cols) {
     if (tile_rows == 32) return r32_smem_bytes(wshift);
-    return (((size_t)1 << wshift) + 1) * D_STRIDE * sizeof(float) + ap_ring_bytes();
+    return (((size_t)1 << wshift) + 1) * D_STRIDE * sizeof(float) +
+           ap_ring_bytes(tile_cols * AP_LPC);
 }
 
-int ap_max_wshift(int tile_rows) { return tile_rows == 32 ? 10 : 11; }
+int ap_max_wshift(int tile_rows, int tile_cols) {
+    (void)tile_cols;
+    return tile_rows == 32 ? 10 : 11;
+}
 
-int ap_threads(uint32_t wshift, int tile_rows) {
+int ap_threads(uint32_t wshift, int tile_rows, int tile_cols) {
     if (tile_rows == 32) return r32_wide(wshift) ? 512 : 256;
-    return AP_THREADS;
+    return tile_cols * AP_LPC;
 }
 
-cudaError_t ap_prepare(uint32_t wshift, int tile_rows, int *ctas_per_sm) {
-    const size_t smem = ap_smem_bytes(wshift, tile_rows);
-    const void *fn;
+static const void *ap_kernel(uint32_t wshift, int tile_rows, int tile_cols) {
     if (tile_rows == 32)
-        fn = r32_wide(wshift) ? (const void *)k_allpairs32<512, 1> : (const void *)k_allpairs32<256, 2>;
-    else
-        fn = (const void *)k_allpairs;
+        return r32_wide(wshift) ? (const void *)k_allpairs32<512, 1>
+                                : (const void *)k_allpairs32<256, 2>;
+    return tile_cols == 32 ? (const void *)k_allpairs<128, 4> : (const void *)k_allpairs<256, 2>;
+}
+
+cudaError_t ap_prepare(uint32_t wshift, int tile_rows, int tile_cols, int *ctas_per_sm) {
+    const size_t smem = ap_smem_bytes(wshift, tile_rows, tile_cols);
+    const void *fn = ap_kernel(wshift, tile_rows, tile_cols);
     PHYLO_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (ctas_per_sm) {
         int n = 0;
         PHYLO_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, fn, ap_threads(wshift, tile_rows), smem));
+            &n, fn, ap_threads(wshift, tile_rows, tile_cols), smem));
         *ctas_per_sm = n;
     }
     return cudaSuccess;
 }
 
-cudaError_t ap_launch(const ApArgs &a, int tile_rows, int grid, cudaStream_t st) {
-    const size_t smem = ap_smem_bytes(a.wshift, tile_rows);
+cudaError_t ap_launch(const ApArgs &a, int tile_rows, int tile_cols, int grid, cudaStream_t st) {
+    const size_t smem = ap_smem_bytes(a.wshift, tile_rows, tile_cols);
     if (tile_rows == 32) {
         if (r32_wide(a.wshift))
             k_allpairs32<512, 1><<<grid, 512, smem, st>>>(a);
         else
             k_allpairs32<256, 2><<<grid, 256, smem, st>>>(a);
+    } else if (tile_cols == 32) {
+        k_allpairs<128, 4><<<grid, 128, smem, st>>>(a);
     } else {
-        k_allpairs<<<grid, AP_THREADS, smem, st>>>(a);
+        k_allpairs<256, 2><<<grid, 256, smem, st>>>(a);
     }
     return cudaGetLastError();
 }
@@ -648,20 +672,20 @@ cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, ui
 // reduction of partial blocks
 // ---------------------------------------------------------------------------
 
-// grid = ntiles, block = 256 (one column per thread)
+// grid = ntiles, block = tile columns (one column per thread)
 __global__ void k_ap_reduce(ApReduceArgs r) {
     const ApTile t = r.tiles[blockIdx.x];
     const uint32_t c = threadIdx.x;
     if (c >= t.ncol) return;
     const uint32_t colid = r.colids[t.col0 + c];
-    const uint64_t blk = (uint64_t)r.ti * AP_TJ;  // float pairs per partial block
+    const uint64_t blk = (uint64_t)r.ti * r.tj;  // float pairs per partial block
     const FF *base = r.part + (uint64_t)blockIdx.x * r.S * blk;
     for (uint32_t i = 0; i < t.nrow; i++) {
         const uint32_t rowpos = t.row0 + i, colpos = t.col0 + c;
         if (r.upper && !(rowpos < colpos)) continue;
         DD acc = {0.0, 0.0};
         for (uint32_t s = 0; s < r.S; s++) {
-            const FF p = base[(uint64_t)s * blk + i * AP_TJ + c];
+            const FF p = base[(uint64_t)s * blk + i * r.tj + c];
             dd_add(acc, (double)p.hi);
             dd_add(acc, (double)p.lo);
         }
@@ -674,7 +698,7 @@ __global__ void k_ap_reduce(ApReduceArgs r) {
 
 cudaError_t ap_reduce_launch(const ApReduceArgs &r, cudaStream_t st) {
     if (r.ntiles == 0) return cudaSuccess;
-    k_ap_reduce<<<r.ntiles, AP_TJ, 0, st>>>(r);
+    k_ap_reduce<<<r.ntiles, r.tj, 0, st>>>(r);
     return cudaGetLastError();
 }
 

@@ -5,17 +5,15 @@
 namespace phylo {
 
 constexpr int AP_TI = 16;             // row vectors per item (densified in shared memory)
-constexpr int AP_THREADS = 256;
 constexpr int AP_LPC = 4;             // lanes per column vector
-constexpr int AP_TJ = AP_THREADS / AP_LPC;  // column vectors per item
 
-// One unit of work: up to 16 row vectors x 64 column vectors over the key
-// windows [w0, w1).  Vectors are named by positions in rowids / colids.
+// One unit of work: up to tile_rows row vectors x tile_cols column vectors over
+// the key windows [w0, w1).  Vectors are named by positions in rowids / colids.
 struct ApItem {
     uint32_t row0, nrow;  // rows: rowids[row0 .. row0 + nrow)
     uint32_t col0, ncol;  // columns: colids[col0 .. col0 + ncol)
     uint32_t w0, w1;      // key windows
-    uint32_t part;        // index of this item's 16 x 256 partial block
+    uint32_t part;        // index of this item's tile_rows x tile_cols partial block
     uint32_t tile;        // tile this item contributes to
 };
 
@@ -36,18 +34,20 @@ struct ApArgs {
     const ApItem *items;
     uint32_t nitems;
     uint32_t *counter;         // work counter (zeroed before launch)
-    FF *part;                  // [parts][tile rows][AP_TJ]
+    FF *part;                  // [parts][tile rows][tile cols]
     uint32_t fold;             // products per accumulator between compensated folds
     int64_t *item_cycles;      // optional per-item clock64 durations (may be null)
 };
 
-// tile_rows selects the kernel: 16 (80-byte records, four lanes per column) or
-// 32 (128-byte swizzled records, eight lanes per column).
-size_t ap_smem_bytes(uint32_t wshift, int tile_rows);
-int ap_max_wshift(int tile_rows);
-int ap_threads(uint32_t wshift, int tile_rows);
-cudaError_t ap_prepare(uint32_t wshift, int tile_rows, int *ctas_per_sm);
-cudaError_t ap_launch(const ApArgs &a, int tile_rows, int grid, cudaStream_t st);
+// Tile shapes (tile_rows x tile_cols) select the kernel: 16 x 64 (256 threads)
+// and 16 x 32 (128 threads) use 80-byte key records and four lanes per column;
+// 32 x 64 uses 128-byte swizzled records and eight lanes per column.
+bool ap_shape_ok(int tile_rows, int tile_cols);
+size_t ap_smem_bytes(uint32_t wshift, int tile_rows, int tile_cols);
+int ap_max_wshift(int tile_rows, int tile_cols);
+int ap_threads(uint32_t wshift, int tile_rows, int tile_cols);
+cudaError_t ap_prepare(uint32_t wshift, int tile_rows, int tile_cols, int *ctas_per_sm);
+cudaError_t ap_launch(const ApArgs &a, int tile_rows, int tile_cols, int grid, cudaStream_t st);
 
 // window index: roff[v][r] = number of entries of vector v with key < r << wshift
 cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
@@ -61,9 +61,9 @@ struct ApTile {
     uint32_t row0, nrow, col0, ncol;
 };
 struct ApReduceArgs {
-    const FF *part;            // blocks of ti x AP_TJ float pairs
+    const FF *part;            // blocks of ti x tj float pairs
     const ApTile *tiles;
-    uint32_t ntiles, S, ti;
+    uint32_t ntiles, S, ti, tj;
     const uint32_t *rowids, *colids;
     double *out;
     uint64_t ldc;

@@ -371,22 +371,21 @@ int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, in
 
 // Sets the kernel's shared-memory limit for this window width and reports the
 // resident CTAs per SM.
-static bool tile_rows_ok(int tile_rows) { return tile_rows == 16 || tile_rows == 32; }
-
-int phyloPairsPrepare(int window_shift, int tile_rows, int *ctas_per_sm) {
-    if (!tile_rows_ok(tile_rows) || window_shift < 4 || window_shift > ap_max_wshift(tile_rows))
+int phyloPairsPrepare(int window_shift, int tile_rows, int tile_cols, int *ctas_per_sm) {
+    if (!ap_shape_ok(tile_rows, tile_cols) || window_shift < 4 ||
+        window_shift > ap_max_wshift(tile_rows, tile_cols))
         return (int)cudaErrorInvalidValue;
-    return (int)ap_prepare((uint32_t)window_shift, tile_rows, ctas_per_sm);
+    return (int)ap_prepare((uint32_t)window_shift, tile_rows, tile_cols, ctas_per_sm);
 }
 
-int phyloPairsSmemBytes(int window_shift, int tile_rows) {
-    if (!tile_rows_ok(tile_rows)) return -1;
-    return (int)ap_smem_bytes((uint32_t)window_shift, tile_rows);
+int phyloPairsSmemBytes(int window_shift, int tile_rows, int tile_cols) {
+    if (!ap_shape_ok(tile_rows, tile_cols)) return -1;
+    return (int)ap_smem_bytes((uint32_t)window_shift, tile_rows, tile_cols);
 }
 
-int phyloPairsThreads(int window_shift, int tile_rows) {
-    if (!tile_rows_ok(tile_rows)) return -1;
-    return ap_threads((uint32_t)window_shift, tile_rows);
+int phyloPairsThreads(int window_shift, int tile_rows, int tile_cols) {
+    if (!ap_shape_ok(tile_rows, tile_cols)) return -1;
+    return ap_threads((uint32_t)window_shift, tile_rows, tile_cols);
 }
 
 // Launches the pair kernel over `num_items` items (8 uint32 each, see ApItem);
@@ -399,8 +398,9 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
                      unsigned int num_windows, int window_shift, uintptr_t d_rowids,
                      uintptr_t d_colids, uintptr_t d_items, int num_items, uintptr_t d_counter,
                      uintptr_t d_part, int fold, uintptr_t d_item_cycles, int tile_rows,
-                     int grid) {
-    if (!tile_rows_ok(tile_rows) || window_shift < 4 || window_shift > ap_max_wshift(tile_rows))
+                     int tile_cols, int grid) {
+    if (!ap_shape_ok(tile_rows, tile_cols) || window_shift < 4 ||
+        window_shift > ap_max_wshift(tile_rows, tile_cols))
         return (int)cudaErrorInvalidValue;
     ApArgs a;
     a.row.keys = (const uint32_t *)d_row_keys;
@@ -422,20 +422,21 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
     // the 16-row kernel adds four products per accumulator between checks
     a.fold = fold >= 4 ? (uint32_t)fold & ~3u : (fold > 0 ? 4u : 28u);
     a.item_cycles = (int64_t *)d_item_cycles;
-    return (int)ap_launch(a, tile_rows, grid, (cudaStream_t)stream);
+    return (int)ap_launch(a, tile_rows, tile_cols, grid, (cudaStream_t)stream);
 }
 
 // Sums the partial blocks of each tile (4 uint32 per tile: row0, nrow, col0, ncol).
 int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
-                     int segments, int tile_rows, uintptr_t d_rowids, uintptr_t d_colids,
-                     uintptr_t d_out, long ldc, int upper, int mirror) {
-    if (!tile_rows_ok(tile_rows)) return (int)cudaErrorInvalidValue;
+                     int segments, int tile_rows, int tile_cols, uintptr_t d_rowids,
+                     uintptr_t d_colids, uintptr_t d_out, long ldc, int upper, int mirror) {
+    if (!ap_shape_ok(tile_rows, tile_cols)) return (int)cudaErrorInvalidValue;
     ApReduceArgs r;
     r.part = (const FF *)d_part;
     r.tiles = (const ApTile *)d_tiles;
     r.ntiles = (uint32_t)num_tiles;
     r.S = (uint32_t)segments;
     r.ti = (uint32_t)tile_rows;
+    r.tj = (uint32_t)tile_cols;
     r.rowids = (const uint32_t *)d_rowids;
     r.colids = (const uint32_t *)d_colids;
     r.out = (double *)d_out;

@@ -297,13 +297,12 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             }
             const bool v2 = run >= K - 2, v1 = run >= K - 1, v0 = run >= K;
             cnt2 += v2; cnt1 += v1; cnt0 += v0;
-            // counts, extension masks and the seen bitmap: reduction atomics only
-            // (no result is waited for; equal keys within a warp are rare, so no
-            // aggregation)
+            // counts and extension masks: reduction atomics (equal keys within a
+            // warp are rare, so no aggregation); the first sighting of a
+            // (K-1)-mer sets its seen bit
             if (v2) atomicAdd(&c2[w2], 1u);
             if (v1) {
-                atomicAdd(&c1[w1], 1u);
-                atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                if (atomicAdd(&c1[w1], 1u) == 0u) atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
                 atomicOr(&mk[w2], 1u << last);
             }
         }

@@ -258,7 +258,8 @@ class PairPlan:
 @dataclass
 class EngineConfig:
     wshift: int = 10
-    tile_rows: int = AP_TI   # 16 or 32 row vectors per work item
+    tile_rows: int = AP_TI   # row vectors per work item (16 or 32)
+    tile_cols: int = AP_TJ   # column vectors per work item (64, or 32 with 16 rows)
     fold: int = 28           # products per FP32 accumulator between compensated folds:
                              # |dC| <= (fold + 2) 2^-24 for unit vectors -> |dD| <= 8.9e-7
     items_per_cta: int = 4
@@ -275,7 +276,8 @@ class PairEngine:
         self.L = _native.load()
         self.device = arena.keys.device
         ctas = ctypes.c_int(0)
-        check(self.L.phyloPairsPrepare(self.cfg.wshift, self.cfg.tile_rows, ctypes.byref(ctas)))
+        check(self.L.phyloPairsPrepare(self.cfg.wshift, self.cfg.tile_rows, self.cfg.tile_cols,
+                                       ctypes.byref(ctas)))
         self.ctas_per_sm = max(1, ctas.value)
         props = torch.cuda.get_device_properties(self.device)
         self.sms = props.multi_processor_count
@@ -389,12 +391,12 @@ class PairEngine:
         perm = ids[order]
         N = len(perm)
         tiles = []
-        ti = self.cfg.tile_rows
+        ti, tj = self.cfg.tile_rows, self.cfg.tile_cols
         for r0 in range(0, N, ti):
             nr = min(ti, N - r0)
             c = r0 + 1
             while c < N:
-                nc = min(AP_TJ, N - c)
+                nc = min(tj, N - c)
                 tiles.append((r0, nr, c, nc))
                 c += nc
         return self._finish_plan(perm, perm, tiles, True, True, ldc or a.n, N * (N - 1) // 2)
@@ -410,17 +412,17 @@ class PairEngine:
         rows = rows[np.argsort(-a.nnz[rows], kind="stable")]
         cols = cols[np.argsort(-ca.nnz[cols], kind="stable")]
         tiles = []
-        ti = self.cfg.tile_rows
+        ti, tj = self.cfg.tile_rows, self.cfg.tile_cols
         for r0 in range(0, len(rows), ti):
             nr = min(ti, len(rows) - r0)
-            for c0 in range(0, len(cols), AP_TJ):
-                tiles.append((r0, nr, c0, min(AP_TJ, len(cols) - c0)))
+            for c0 in range(0, len(cols), tj):
+                tiles.append((r0, nr, c0, min(tj, len(cols) - c0)))
         return self._finish_plan(rows, cols, tiles, False, False, ldc, len(rows) * len(cols),
                                  a.nnz, ca.nnz)
 
     # -- execution -------------------------------------------------------------
     def _parts(self, plan: PairPlan) -> torch.Tensor:
-        need = plan.ntiles * plan.S * self.cfg.tile_rows * AP_TJ * 2
+        need = plan.ntiles * plan.S * self.cfg.tile_rows * self.cfg.tile_cols * 2
         if self.part is None or self.part.numel() < need:
             self.part = torch.empty(need, dtype=torch.float32, device=self.device)
         return self.part
@@ -446,11 +448,11 @@ class PairEngine:
             _p(ca.values), _p(ca.vec_off), _p(ca.roff), a.R, self.cfg.wshift,
             _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems, _p(self.counter),
             _p(part), self.cfg.fold, _p(item_cycles) if item_cycles is not None else 0,
-            self.cfg.tile_rows, self.grid))
+            self.cfg.tile_rows, self.cfg.tile_cols, self.grid))
         if events is not None:
             events[1].record(s_obj)
         check(self.L.phyloPairsReduce(
-            st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, self.cfg.tile_rows,
+            st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, self.cfg.tile_rows, self.cfg.tile_cols,
             _p(plan.rowids), _p(plan.colids), _p(out), plan.ldc, int(plan.upper),
             int(plan.mirror)))
         self.launches += 3  # counter fill, pair kernel, reduction
@@ -577,12 +579,13 @@ def tune_key(arena: Arena, n_rows: int, n_cols: int) -> str:
 
 
 TUNE_SPACE = [
-    dict(wshift=10, tile_rows=16, fold=28, items_per_cta=4),
-    dict(wshift=10, tile_rows=16, fold=28, items_per_cta=2),
-    dict(wshift=10, tile_rows=16, fold=28, items_per_cta=8),
-    dict(wshift=9, tile_rows=16, fold=28, items_per_cta=4),
-    dict(wshift=11, tile_rows=16, fold=28, items_per_cta=4),
-    dict(wshift=10, tile_rows=32, fold=28, items_per_cta=4),
+    dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
+    dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=2),
+    dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=8),
+    dict(wshift=9, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
+    dict(wshift=11, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
+    dict(wshift=9, tile_rows=16, tile_cols=32, fold=28, items_per_cta=4),
+    dict(wshift=10, tile_rows=32, tile_cols=64, fold=28, items_per_cta=4),
 ]
 
 

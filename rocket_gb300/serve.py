@@ -38,7 +38,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .engine import AP_TJ, Arena, BatchBuilder, EngineConfig, PairEngine, key_limit
+from .engine import Arena, BatchBuilder, EngineConfig, PairEngine, key_limit
 from .synth import Proteomes
 
 
@@ -244,8 +244,9 @@ class ServingEngine:
         staged = float(np.sum(8 * lens + 64)) * 8.0
         roff = nq * (self.db.R + 1) * 4.0
         ti = self.cfg.tile_rows
-        tiles = math.ceil(nq / ti) * math.ceil(max(db_n, 1) / AP_TJ)
-        parts = tiles * self.cfg.segments * ti * AP_TJ * 8.0
+        tj = self.cfg.tile_cols
+        tiles = math.ceil(nq / ti) * math.ceil(max(db_n, 1) / tj)
+        parts = tiles * self.cfg.segments * ti * tj * 8.0
         out = nq * max(db_n, 1) * 8.0
         return scratch + staged + roff + parts + out
 

@@ -69,7 +69,9 @@ def test_batch_scratch_rejects_bad_arguments(lib):
     assert f("dna", 6, 4, 1000) == -1
     assert f("DNA", 10, 4, 1000) > 0
     assert lib.phyloBuildLaunchesPerBatch() > 0
-    assert lib.phyloPairsSmemBytes(10, 16) == (1024 + 1) * 80 + 2 * 256 * 32  # table + ring
-    assert lib.phyloPairsSmemBytes(10, 32) == (1024 + 1) * 128
-    assert lib.phyloPairsSmemBytes(10, 24) == -1
-    assert lib.phyloPairsThreads(10, 32) == 512 and lib.phyloPairsThreads(9, 32) == 256
+    assert lib.phyloPairsSmemBytes(10, 16, 64) == (1024 + 1) * 80 + 2 * 256 * 32  # table + ring
+    assert lib.phyloPairsSmemBytes(9, 16, 32) == (512 + 1) * 80 + 2 * 128 * 32
+    assert lib.phyloPairsSmemBytes(10, 32, 64) == (1024 + 1) * 128
+    assert lib.phyloPairsSmemBytes(10, 24, 64) == -1 and lib.phyloPairsSmemBytes(10, 32, 32) == -1
+    assert lib.phyloPairsThreads(10, 32, 64) == 512 and lib.phyloPairsThreads(9, 32, 64) == 256
+    assert lib.phyloPairsThreads(10, 16, 64) == 256 and lib.phyloPairsThreads(9, 16, 32) == 128
