@@ -83,7 +83,10 @@ __device__ __forceinline__ void fold16(float (&acc)[16], float (&hi)[16], float 
 // Per-thread ring of 16-byte column groups (4 keys + 4 values) fetched with
 // cp.async, RING groups ahead of the one being used, so a thread's column stream
 // stays in flight across window barriers.
-constexpr int RING = 2;
+#ifndef AP_RING
+#define AP_RING 2
+#endif
+constexpr int RING = AP_RING;
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem)
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                 cp_async16(&ring_v[slot_fetch * THREADS + threadIdx.x], a.col.vals + cbase + fetch);
             }
             fetch += 4 * AP_LPC;
-            slot_fetch = (slot_fetch + 1) & (RING - 1);
+            slot_fetch = slot_fetch + 1 == RING ? 0 : slot_fetch + 1;
             cp_async_commit();
         }
 
@@ -279,10 +282,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                                    a.col.vals + cbase + fetch);
                     }
                     fetch += 4 * AP_LPC;
-                    slot_fetch = (slot_fetch + 1) & (RING - 1);
+                    slot_fetch = slot_fetch + 1 == RING ? 0 : slot_fetch + 1;
                     cp_async_commit();
                     cur += 4 * AP_LPC;
-                    slot_cur = (slot_cur + 1) & (RING - 1);
+                    slot_cur = slot_cur + 1 == RING ? 0 : slot_cur + 1;
                 }
             }
             c_lo = c_hi;
