@@ -556,8 +556,8 @@ def main():
                     help="pair kernel on raw keys instead of dense key ranks")
     ap.add_argument("--tile-rows", type=int, default=16, choices=[16, 32],
                     help="row vectors per pair-kernel work item (selects the kernel)")
-    ap.add_argument("--tile-cols", type=int, default=64, choices=[32, 64],
-                    help="column vectors per pair-kernel work item (32: 128-thread CTAs)")
+    ap.add_argument("--tile-cols", type=int, default=64, choices=[32, 64, 128],
+                    help="column vectors per pair-kernel work item (4 threads per column)")
     ap.add_argument("--fold", type=int, default=28,
                     help="products per FP32 accumulator between compensated folds (multiple of 4)")
     ap.add_argument("--items-per-cta", type=int, default=4)

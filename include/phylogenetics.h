@@ -150,7 +150,7 @@ int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, in
                      uintptr_t d_roff);
 
 /* The tile shape (tile_rows x tile_cols row x column vectors per work item)
- * selects the pair kernel: 16 x 64 (256 threads) or 16 x 32 (128 threads) use
+ * selects the pair kernel: 16 x 128, 16 x 64 or 16 x 32 (512, 256 or 128 threads) use
  * 80-byte key records and four lanes per column vector, windows up to 2^11
  * keys; 32 x 64 uses 128-byte swizzled records and eight lanes per column
  * vector, windows up to 2^10 keys.  Partial blocks are tile_rows x tile_cols

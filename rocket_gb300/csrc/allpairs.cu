@@ -569,7 +569,7 @@ static size_t r32_smem_bytes(uint32_t wshift) {
 static bool r32_wide(uint32_t wshift) { return r32_smem_bytes(wshift) > 100 * 1024; }
 
 bool ap_shape_ok(int tile_rows, int tile_cols) {
-    return (tile_rows == 16 && (tile_cols == 64 || tile_cols == 32)) ||
+    return (tile_rows == 16 && (tile_cols == 128 || tile_cols == 64 || tile_cols == 32)) ||
            (tile_rows == 32 && tile_cols == 64);
 }
 
@@ -593,6 +593,7 @@ static const void *ap_kernel(uint32_t wshift, int tile_rows, int tile_cols) {
     if (tile_rows == 32)
         return r32_wide(wshift) ? (const void *)k_allpairs32<512, 1>
                                 : (const void *)k_allpairs32<256, 2>;
+    if (tile_cols == 128) return (const void *)k_allpairs<512, 1>;
     return tile_cols == 32 ? (const void *)k_allpairs<128, 4> : (const void *)k_allpairs<256, 2>;
 }
 
@@ -616,6 +617,8 @@ cudaError_t ap_launch(const ApArgs &a, int tile_rows, int tile_cols, int grid, c
             k_allpairs32<512, 1><<<grid, 512, smem, st>>>(a);
         else
             k_allpairs32<256, 2><<<grid, 256, smem, st>>>(a);
+    } else if (tile_cols == 128) {
+        k_allpairs<512, 1><<<grid, 512, smem, st>>>(a);
     } else if (tile_cols == 32) {
         k_allpairs<128, 4><<<grid, 128, smem, st>>>(a);
     } else {

@@ -39,8 +39,8 @@ struct ApArgs {
     int64_t *item_cycles;      // optional per-item clock64 durations (may be null)
 };
 
-// Tile shapes (tile_rows x tile_cols) select the kernel: 16 x 64 (256 threads)
-// and 16 x 32 (128 threads) use 80-byte key records and four lanes per column;
+// Tile shapes (tile_rows x tile_cols) select the kernel: 16 x 128 (512 threads),
+// 16 x 64 (256) and 16 x 32 (128) use 80-byte key records and four lanes per column;
 // 32 x 64 uses 128-byte swizzled records and eight lanes per column.
 bool ap_shape_ok(int tile_rows, int tile_cols);
 size_t ap_smem_bytes(uint32_t wshift, int tile_rows, int tile_cols);

@@ -75,3 +75,4 @@ def test_batch_scratch_rejects_bad_arguments(lib):
     assert lib.phyloPairsSmemBytes(10, 24, 64) == -1 and lib.phyloPairsSmemBytes(10, 32, 32) == -1
     assert lib.phyloPairsThreads(10, 32, 64) == 512 and lib.phyloPairsThreads(9, 32, 64) == 256
     assert lib.phyloPairsThreads(10, 16, 64) == 256 and lib.phyloPairsThreads(9, 16, 32) == 128
+    assert lib.phyloPairsThreads(11, 16, 128) == 512

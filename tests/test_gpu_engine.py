@@ -60,7 +60,8 @@ def test_allpairs_matches_fp64(small, wshift, fold, rows, compress):
 
 
 @pytest.mark.parametrize("wshift,rows,cols", [(10, 32, 64), (9, 32, 64), (10, 16, 64),
-                                              (9, 16, 32), (10, 16, 32)])
+                                              (9, 16, 32), (10, 16, 32), (11, 16, 128),
+                                              (10, 16, 128)])
 def test_allpairs_many_tiles(many, wshift, rows, cols):
     p, arena, C_ref = many
     eng = PairEngine(arena, EngineConfig(wshift=wshift, tile_rows=rows, tile_cols=cols))
