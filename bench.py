@@ -410,9 +410,8 @@ def run_ours(args):
     peak, peak_kind = _peaks()
     k_ms = float(np.mean(kernel_ms))
     achieved = alg_bytes / (k_ms / 1000.0) / 1e9
-    kernel_name = "k_allpairs32" if args.tile_rows == 32 else "k_allpairs"
-    if args.tile_rows == 16 and args.tile_cols != 64:
-        kernel_name += f"_c{args.tile_cols}"
+    kernel_name = ("k_allpairs32" if args.tile_rows == 32 else "k_allpairs") + \
+        f"_{args.tile_rows}x{args.tile_cols}"
     traffic = _traffic_per_launch(kernel_name, args.workload, args.wshift)
     line = {
         "metric": "pairwise CV distances/s", "value": value, "unit": "pairs/s",
@@ -551,12 +550,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--wshift", type=int, default=10)
+    ap.add_argument("--wshift", type=int, default=11)
     ap.add_argument("--no-compress", action="store_true",
                     help="pair kernel on raw keys instead of dense key ranks")
     ap.add_argument("--tile-rows", type=int, default=16, choices=[16, 32],
                     help="row vectors per pair-kernel work item (selects the kernel)")
-    ap.add_argument("--tile-cols", type=int, default=64, choices=[32, 64, 128],
+    ap.add_argument("--tile-cols", type=int, default=128, choices=[32, 64, 128],
                     help="column vectors per pair-kernel work item (4 threads per column)")
     ap.add_argument("--fold", type=int, default=28,
                     help="products per FP32 accumulator between compensated folds (multiple of 4)")

@@ -30,7 +30,7 @@ from . import _native
 from ._native import check
 
 AP_TI = 16          # default rows per work item (16 or 32: selects the pair kernel)
-AP_TJ = 64
+AP_TJ = 128         # default column vectors per work item (512-thread CTAs)
 NSYM = {"protein": 21, "DNA": 4}
 
 
@@ -257,9 +257,9 @@ class PairPlan:
 
 @dataclass
 class EngineConfig:
-    wshift: int = 10
+    wshift: int = 11
     tile_rows: int = AP_TI   # row vectors per work item (16 or 32)
-    tile_cols: int = AP_TJ   # column vectors per work item (64, or 32 with 16 rows)
+    tile_cols: int = AP_TJ   # column vectors per work item (128, 64 or 32; 64 with 32 rows)
     fold: int = 28           # products per FP32 accumulator between compensated folds:
                              # |dC| <= (fold + 2) 2^-24 for unit vectors -> |dD| <= 8.9e-7
     items_per_cta: int = 4
@@ -579,6 +579,8 @@ def tune_key(arena: Arena, n_rows: int, n_cols: int) -> str:
 
 
 TUNE_SPACE = [
+    dict(wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=4),
+    dict(wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=8),
     dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
     dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=2),
     dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=8),
