@@ -145,11 +145,13 @@ def _dist():
 
 
 def _barrier_max(value: float, world: int) -> float:
+    """Maximum of `value` over the ranks (the slowest replica sets the time)."""
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

@@ -276,6 +276,9 @@ class PairEngine:
         self.L = _native.load()
         self.device = arena.keys.device
         ctas = ctypes.c_int(0)
+        if self.L.phyloPairsSmemBytes(self.cfg.wshift, self.cfg.tile_rows, self.cfg.tile_cols) < 0:
+            raise ValueError(f"unsupported pair tile {self.cfg.tile_rows} x {self.cfg.tile_cols} "
+                             "(16 x 128, 16 x 64, 16 x 32 or 32 x 64)")
         check(self.L.phyloPairsPrepare(self.cfg.wshift, self.cfg.tile_rows, self.cfg.tile_cols,
                                        ctypes.byref(ctas)))
         self.ctas_per_sm = max(1, ctas.value)

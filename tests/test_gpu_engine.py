@@ -44,6 +44,7 @@ def many():
 def test_allpairs_matches_fp64(small, wshift, fold, rows, compress):
     p, arena, C_ref = small
     eng = PairEngine(arena, EngineConfig(wshift=wshift, fold=fold, tile_rows=rows,
+                                         tile_cols=64 if rows == 32 else 128,
                                          compress=compress))
     eng.ensure_index()
     plan = eng.plan_triangle()
@@ -170,3 +171,20 @@ def test_autotune(small, tmp_path, monkeypatch):
     assert r["algorithm"] in ("window", "merge") and r["ms"] > 0
     assert len(r["candidates"]) >= 2
     assert autotune(arena)["ms"] == r["ms"]  # served from the cache
+
+
+def test_directory_driver(tmp_path):
+    """The command-line driver: FASTA files in, all-pair JSON out (C, -1 nowhere)."""
+    import json
+    from rocket_gb300.output import main
+    p = synth.workload("uneven1024", n=5, scale=0.01)
+    for i in range(len(p)):
+        seq = p.get(i).decode().split("\n")
+        (tmp_path / f"g{i}.faa").write_text("".join(f">p{j}\n{s}\n" for j, s in enumerate(seq) if s))
+    out = tmp_path / "out.json"
+    assert main([str(tmp_path), str(out)]) == 0
+    d = json.loads(out.read_text())
+    C = np.array(d["distance"])
+    assert d["files"] == [f"g{i}.faa" for i in range(5)]
+    C_ref = oracle_matrix(p)
+    assert np.abs(C - C_ref).max() <= 2e-6
