@@ -262,7 +262,7 @@ class EngineConfig:
     tile_cols: int = AP_TJ   # column vectors per work item (128, 64 or 32; 64 with 32 rows)
     fold: int = 28           # products per FP32 accumulator between compensated folds:
                              # |dC| <= (fold + 2) 2^-24 for unit vectors -> |dD| <= 8.9e-7
-    items_per_cta: int = 4
+    items_per_cta: int = 8
     min_windows_per_item: int = 64
     segments: int = 0        # key segments per tile; 0 = chosen from the plan size.  A fixed
                              # value makes each pair's arithmetic independent of the plan.
