@@ -320,7 +320,8 @@ def run_ours(args):
     pinned = torch.from_numpy(wl.data).pin_memory()
     seq = torch.empty(pinned.numel(), dtype=torch.uint8, device=dev)
     seq.copy_(pinned)
-    builder = BatchBuilder("protein", args.k, device=dev, max_batch=args.max_batch)
+    builder = BatchBuilder("protein", args.k, device=dev, max_batch=args.max_batch,
+                           overlap=not args.no_overlap)
     cfg = EngineConfig(wshift=args.wshift, fold=args.fold, items_per_cta=args.items_per_cta,
                        tile_rows=args.tile_rows, tile_cols=args.tile_cols,
                        compress=not args.no_compress)
@@ -553,6 +554,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--wshift", type=int, default=11)
+    ap.add_argument("--no-overlap", action="store_true",
+                    help="build one batch at a time instead of two in flight")
     ap.add_argument("--no-compress", action="store_true",
                     help="pair kernel on raw keys instead of dense key ranks")
     ap.add_argument("--tile-rows", type=int, default=16, choices=[16, 32],

@@ -112,6 +112,18 @@ int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size
                         uintptr_t d_seq_off, long max_candidates, int64_t *h_nnz,
                         int64_t *h_candidates);
 
+/* Phase 1 without waiting for it: the Plan's kernels, then asynchronous
+ * copies of the results into h_summary, a pinned host buffer of
+ * phyloBuildBatchSummaryBytes bytes laid out as int64 nnz[num_proteomes] |
+ * float64 norm[num_proteomes] | int64 candidate slots needed | uint32 status
+ * (bit 1: candidate capacity exceeded; retry with a larger max_candidates).
+ * Read it only after the stream (or an event recorded after this call) has
+ * completed.  Lets a caller overlap the builds of two batches on two streams. */
+int phyloBuildBatchPlanAsync(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                             const char *alphabet, int k, int num_proteomes, uintptr_t d_seq,
+                             uintptr_t d_seq_off, long max_candidates, void *h_summary);
+long phyloBuildBatchSummaryBytes(int num_proteomes);
+
 /* Phase 2 (same scratch and arguments as the Plan): vector p is written at
  * d_keys/d_values[vec_off[p] ..] with vec_off[p] = arena_base + earlier sizes
  * rounded up to 4 entries; d_vec_off (uint64[num_proteomes + 1]) receives the

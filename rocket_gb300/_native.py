@@ -69,6 +69,11 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloBuildBatchPlan.argtypes = [c_ptr, c_ptr, c_long, c_char_p, c_int, c_int, c_ptr, c_ptr,
                                       c_long, c_ptr, c_ptr]
     L.phyloBuildBatchPlan.restype = c_int
+    L.phyloBuildBatchPlanAsync.argtypes = [c_ptr, c_ptr, c_long, c_char_p, c_int, c_int, c_ptr,
+                                           c_ptr, c_long, c_ptr]
+    L.phyloBuildBatchPlanAsync.restype = c_int
+    L.phyloBuildBatchSummaryBytes.argtypes = [c_int]
+    L.phyloBuildBatchSummaryBytes.restype = c_long
     L.phyloBuildBatchEmit.argtypes = [c_ptr, c_ptr, c_long, c_char_p, c_int, c_int, c_long, c_ptr,
                                       c_ptr, c_ptr, c_long, c_ptr]
     L.phyloBuildBatchEmit.restype = c_int
@@ -118,7 +123,8 @@ def _declare(L: ctypes.CDLL) -> None:
 # Every symbol that include/phylogenetics.h declares.
 EXPORTED = [
     "estimateScratchMemory", "buildCompositionVector", "compareCompositionVectors",
-    "compareCompositionVectorsStatic", "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchEmit", "phyloBuildBatchNorms",
+    "compareCompositionVectorsStatic", "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchPlanAsync",
+    "phyloBuildBatchSummaryBytes", "phyloBuildBatchEmit", "phyloBuildBatchNorms",
     "phyloBuildBatchCounts", "phyloBuildLaunchesPerBatch", "phyloWindowIndex",
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsThreads", "phyloPairsLaunch",
     "phyloPairsReduce",

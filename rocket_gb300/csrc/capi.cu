@@ -280,6 +280,42 @@ int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size
     return (int)cudaGetLastError();
 }
 
+// Phase 1 without waiting: the same kernels, then copies of the results into
+// the caller's pinned host buffer h_summary (see the header); the caller
+// synchronises the stream (or an event recorded after this call) before
+// reading it.
+int phyloBuildBatchPlanAsync(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
+                             const char *alphabet, int k, int num_proteomes, uintptr_t d_seq,
+                             uintptr_t d_seq_off, long max_candidates, void *h_summary) {
+    const int alpha = parse_alphabet(alphabet);
+    BuildGeometry g;
+    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0 || !h_summary) {
+        fprintf(stderr, "error: invalid batch build arguments (alphabet %s, k=%d, n=%d)\n",
+                alphabet ? alphabet : "(null)", k, num_proteomes);
+        return (int)cudaErrorInvalidValue;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    BuildArgs a;
+    memset(&a, 0, sizeof(a));
+    PHYLO_CHECK(build_carve(g, num_proteomes, (uint64_t)max_candidates, (void *)d_scratch,
+                            (size_t)scratch_size, &a));
+    a.seq = (const uint8_t *)d_seq;
+    a.seq_off = (const uint64_t *)d_seq_off;
+    PHYLO_CHECK(build_plan(a, st));
+    // summary layout: int64 nnz[B] | float64 norm[B] | int64 candidates | uint32 status
+    char *h = (char *)h_summary;
+    const size_t B = (size_t)num_proteomes;
+    PHYLO_CHECK(cudaMemcpyAsync(h, a.nnz, 8 * B, cudaMemcpyDeviceToHost, st));
+    PHYLO_CHECK(cudaMemcpyAsync(h + 8 * B, a.norm, 8 * B, cudaMemcpyDeviceToHost, st));
+    PHYLO_CHECK(cudaMemcpyAsync(h + 16 * B, a.cand_total, 8, cudaMemcpyDeviceToHost, st));
+    PHYLO_CHECK(cudaMemcpyAsync(h + 16 * B + 8, a.status, 4, cudaMemcpyDeviceToHost, st));
+    return (int)cudaGetLastError();
+}
+
+long phyloBuildBatchSummaryBytes(int num_proteomes) {
+    return num_proteomes > 0 ? 16L * num_proteomes + 16 : -1;
+}
+
 // Phase 2 (after Plan, same scratch): writes vector p at
 // d_keys/d_values[vec_off[p] ..], vec_off[p] = arena_base + sum of earlier sizes
 // rounded up to 4 entries; d_vec_off (uint64[num_proteomes + 1]) receives the

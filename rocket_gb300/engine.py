@@ -121,24 +121,41 @@ def _grow(t: torch.Tensor, n: int) -> torch.Tensor:
 
 
 class BatchBuilder:
-    """Builds composition vectors of many proteomes into an :class:`Arena`."""
+    """Builds composition vectors of many proteomes into an :class:`Arena`.
 
-    def __init__(self, alphabet: str = "protein", k: int = 6, device=None, max_batch: int = 64):
+    Batches of up to ``max_batch`` proteomes; with ``overlap`` two batches are in
+    flight at once, on the caller's stream and a second stream with their own
+    scratch, so that one batch's kernels fill the gaps of the other's."""
+
+    def __init__(self, alphabet: str = "protein", k: int = 6, device=None, max_batch: int = 64,
+                 overlap: bool = True):
         self.alphabet = alphabet
         self.k = k
         self.device = torch.device(device if device is not None else "cuda")
         self.max_batch = max_batch
+        self.overlap = overlap
         self.L = _native.load()
-        self._scratch = None
+        self._scratch = [None, None]
+        self._summary = [None, None]
+        self._side = None
         self.launches = 0
 
-    def _scratch_for(self, B: int, cand_cap: int) -> torch.Tensor:
+    def _scratch_for(self, slot: int, B: int, cand_cap: int) -> torch.Tensor:
         n = int(self.L.phyloBuildBatchScratch(self.alphabet.encode(), self.k, B, cand_cap))
         if n < 0:
             raise ValueError(f"invalid build geometry: alphabet={self.alphabet} k={self.k}")
-        if self._scratch is None or self._scratch.numel() < n:
-            self._scratch = torch.empty(n, dtype=torch.uint8, device=self.device)
-        return self._scratch
+        if self._scratch[slot] is None or self._scratch[slot].numel() < n:
+            if self._scratch[slot] is not None:
+                torch.cuda.synchronize(self.device)  # queued work may still use the old one
+            self._scratch[slot] = None
+            self._scratch[slot] = torch.empty(n, dtype=torch.uint8, device=self.device)
+        return self._scratch[slot]
+
+    def _summary_for(self, slot: int) -> torch.Tensor:
+        n = int(self.L.phyloBuildBatchSummaryBytes(self.max_batch))
+        if self._summary[slot] is None or self._summary[slot].numel() < n:
+            self._summary[slot] = torch.empty(n, dtype=torch.uint8).pin_memory()
+        return self._summary[slot]
 
     def new_arena(self, capacity_entries: int, capacity_vectors: int) -> Arena:
         keys = torch.empty(max(int(capacity_entries), 4), dtype=torch.int32, device=self.device)
@@ -150,7 +167,8 @@ class BatchBuilder:
     def build(self, seq: torch.Tensor, seq_off: np.ndarray, arena: Optional[Arena] = None,
               stream: Optional[torch.cuda.Stream] = None) -> Arena:
         """Builds the proteomes seq[seq_off[i]:seq_off[i+1]] (seq on the device) and
-        appends them to ``arena`` (a new one if None)."""
+        appends them to ``arena`` (a new one if None).  Work is ordered on ``stream``
+        (default: the current stream): later work on it sees the whole build."""
         seq_off = np.asarray(seq_off, np.int64)
         n = len(seq_off) - 1
         lens = np.diff(seq_off)
@@ -166,48 +184,85 @@ class BatchBuilder:
     def _build_into(self, arena: Arena, seq: torch.Tensor, seq_off: np.ndarray, lens: np.ndarray,
                     stream: torch.cuda.Stream) -> None:
         n = len(seq_off) - 1
-        st = int(stream.cuda_stream)
         d_seq_off_all = torch.from_numpy(seq_off).to(self.device, non_blocking=False)
-        first = 0
-        while first < n:
-            B = min(self.max_batch, n - first)
-            sl = slice(first, first + B)
-            lens_b = lens[sl]
+        batches = [(f, min(self.max_batch, n - f)) for f in range(0, n, self.max_batch)]
+        overlap = self.overlap and len(batches) > 1
+        streams = [stream]
+        if overlap:
+            if self._side is None:
+                self._side = torch.cuda.Stream(self.device)
+            start = torch.cuda.Event()
+            start.record(stream)
+            self._side.wait_event(start)
+            streams.append(self._side)
+        keep = []  # device tensors used by queued work, held until the build is joined
+
+        def enqueue(bi: int) -> dict:
+            first, B = batches[bi]
+            slot = bi % len(streams)
+            st = streams[slot]
+            lens_b = lens[first:first + B]
             cand = int(np.sum(np.minimum(8 * lens_b + 65536, key_limit(self.alphabet, self.k))))
-            # offsets of this sub-batch relative to its first proteome
             base = int(seq_off[first])
-            d_off = d_seq_off_all[first:first + B + 1] - base
+            with torch.cuda.stream(st):
+                d_off = d_seq_off_all[first:first + B + 1] - base
+                scr = self._scratch_for(slot, B, cand)
             d_seq = seq[base:int(seq_off[first + B])]
-            nnz = np.zeros(B, np.int64)
-            total_cand = np.zeros(1, np.int64)
-            for attempt in range(2):
-                scr = self._scratch_for(B, cand)
-                rc = self.L.phyloBuildBatchPlan(
-                    st, _p(scr), scr.numel(), self.alphabet.encode(), self.k, B,
-                    _p(d_seq) if d_seq.numel() else _p(seq), _p(d_off), cand,
-                    nnz.ctypes.data, total_cand.ctypes.data)
-                if rc == 2 and attempt == 0:  # capacity: retry with the exact count
-                    cand = int(total_cand[0])
-                    continue
-                check(rc)
-                break
+            keep.append(d_off)
+            summ = self._summary_for(slot)
+            check(self.L.phyloBuildBatchPlanAsync(
+                int(st.cuda_stream), _p(scr), scr.numel(), self.alphabet.encode(), self.k, B,
+                _p(d_seq) if d_seq.numel() else _p(seq), _p(d_off), cand, summ.data_ptr()))
+            ev = torch.cuda.Event()
+            ev.record(st)
+            return dict(bi=bi, slot=slot, st=st, B=B, first=first, cand=cand, ev=ev, scr=scr,
+                        d_off=d_off, d_seq=d_seq)
+
+        def finish(p: dict) -> None:
+            B, st, scr = p["B"], p["st"], p["scr"]
+            p["ev"].synchronize()
+            raw = self._summary[p["slot"]].numpy()
+            nnz = raw[:8 * B].view(np.int64).copy()
+            norms = raw[8 * B:16 * B].view(np.float64).copy()
+            needed = int(raw[16 * B:16 * B + 8].view(np.int64)[0])
+            status = int(raw[16 * B + 8:16 * B + 12].view(np.uint32)[0])
+            cand = p["cand"]
+            if status & 2:  # candidate capacity: redo this batch with the exact count
+                torch.cuda.synchronize(self.device)
+                cand = needed
+                with torch.cuda.stream(st):
+                    scr = self._scratch_for(p["slot"], B, cand)
+                d_seq = p["d_seq"]
+                total_cand = np.zeros(1, np.int64)
+                check(self.L.phyloBuildBatchPlan(
+                    int(st.cuda_stream), _p(scr), scr.numel(), self.alphabet.encode(), self.k, B,
+                    _p(d_seq) if d_seq.numel() else _p(seq), _p(p["d_off"]), cand,
+                    nnz.ctypes.data, total_cand.ctypes.data))
+                check(self.L.phyloBuildBatchNorms(int(st.cuda_stream), _p(scr), scr.numel(),
+                                                  self.alphabet.encode(), self.k, B, cand,
+                                                  norms.ctypes.data))
             self.launches += int(self.L.phyloBuildLaunchesPerBatch())
-            norms = np.zeros(B, np.float64)
-            check(self.L.phyloBuildBatchNorms(st, _p(scr), scr.numel(), self.alphabet.encode(),
-                                              self.k, B, cand, norms.ctypes.data))
             padded = (nnz + 3) // 4 * 4
             need = arena.used + int(padded.sum()) + 4
             if arena.keys.numel() < need:
+                torch.cuda.synchronize(self.device)  # queued emits write the old buffers
                 cap = int(max(need, arena.keys.numel() * 1.5))
                 arena.keys = _grow(arena.keys, cap)
                 arena.values = _grow(arena.values, cap)
+                if arena.rkeys is not None:
+                    arena.rkeys = None
             # mark the union bitmap for dense key ranks while every vector is marked
             mark = arena.union_n == arena.n
             if mark and arena.union_bits is None:
                 nb = int(self.L.phyloKeyRankBitmapBytes(key_limit(self.alphabet, self.k)))
-                arena.union_bits = torch.zeros(nb // 4, dtype=torch.int32, device=self.device)
+                with torch.cuda.stream(stream):
+                    arena.union_bits = torch.zeros(nb // 4, dtype=torch.int32, device=self.device)
+                if overlap:
+                    ev = torch.cuda.Event()
+                    ev.record(stream)
+                    st.wait_event(ev)
             check(self.L.phyloBuildBatchEmit(
-                st, _p(scr), scr.numel(), self.alphabet.encode(), self.k, B, cand,
+                int(st.cuda_stream), _p(scr), scr.numel(), self.alphabet.encode(), self.k, B, cand,
                 _p(arena.keys), _p(arena.values), _p(arena.vec_off[arena.n:]), arena.used,
                 _p(arena.union_bits) if mark else 0))
             if mark:
@@ -217,7 +272,25 @@ class BatchBuilder:
             new_off = arena.used + np.concatenate([[0], np.cumsum(padded)])
             arena.off = np.concatenate([arena.off[:arena.n], new_off])
             arena.n += B
-            first += B
+
+        prev = None
+        for bi in range(len(batches)):
+            cur = enqueue(bi)
+            if prev is not None:
+                finish(prev)
+            if not overlap:
+                finish(cur)
+                cur = None
+            prev = cur
+        if prev is not None:
+            finish(prev)
+        if overlap:
+            done = torch.cuda.Event()
+            done.record(self._side)
+            stream.wait_event(done)
+            # tensors the side stream used stay alive until it has finished with them
+            for t in keep:
+                t.record_stream(self._side)
 
 
 def upload_proteomes(data: np.ndarray, device=None, pinned: Optional[torch.Tensor] = None,
