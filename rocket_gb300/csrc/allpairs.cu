@@ -86,6 +86,10 @@ __device__ __forceinline__ void fold16(float (&acc)[16], float (&hi)[16], float 
 #ifndef AP_RING
 #define AP_RING 2
 #endif
+// Row entries per lane prefetched into registers for the next window (at least).
+#ifndef AP_NPF
+#define AP_NPF 2
+#endif
 constexpr int RING = AP_RING;
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -116,7 +120,7 @@ struct ApShape {
     static constexpr int TJ = THREADS / AP_LPC;  // column vectors per item
     static constexpr int RPW = AP_TI / NW;       // rows a warp scatters
     static constexpr int LPR = 32 / RPW;         // lanes per scattered row
-    static constexpr int NPF = RPW;              // prefetched entries per lane (NPF * LPR = 32)
+    static constexpr int NPF = RPW < AP_NPF ? AP_NPF : RPW;  // prefetched entries per lane
 };
 
 // Column side: four lanes per column vector.  Lane q of a column streams the
@@ -124,8 +128,8 @@ struct ApShape {
 // lanes of a column fetch 64 contiguous bytes per load, and keeps its own 16
 // accumulators for the whole item; the four lanes' sums are combined once, at
 // the end of the item.  Row side: lane (srow, sj) of a warp scatters entries
-// sj, sj + LPR, ... of row warp * RPW + srow; the first 32 entries of each row's
-// next window are prefetched into registers.
+// sj, sj + LPR, ... of row warp * RPW + srow; the first NPF * LPR entries of each
+// row's next window are prefetched into registers.
 template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
     using S = ApShape<THREADS>;
@@ -188,8 +192,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
         for (int i = 0; i < 16; i++) acc[i] = hi[i] = lo[i] = 0.0f;
         uint32_t nacc = 0;
 
-        // window offsets of LPR windows, held by the row's lanes; the first 32
-        // entries of the row's next window prefetched, NPF per lane
+        // window offsets of LPR windows, held by the row's lanes; the first
+        // NPF * LPR entries of the row's next window prefetched, NPF per lane
         uint32_t wb = item.w0;
         uint32_t r_lo = 0, r_hi = 0;
         if (has_row) {
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
             const int sl = (int)(r - wb);
             const uint32_t lo_r = __shfl_sync(0xffffffffu, r_lo, rsrc + sl);
             const uint32_t hi_r = __shfl_sync(0xffffffffu, r_hi, rsrc + sl);
-            // scatter window r of row rr: first 32 entries from registers, the rest loaded
+            // scatter window r of row rr: first NPF * LPR entries from registers, the rest loaded
             uint32_t ck[NPF];
 #pragma unroll
             for (int t = 0; t < NPF; t++) {
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                 if (pk[t] != 0xffffffffu) D[d_slot(pk[t] & wmask, rr)] = pv[t];
             }
             if (has_row) {
-                for (uint32_t e = lo_r + 32 + sj; e < hi_r; e += LPR) {
+                for (uint32_t e = lo_r + NPF * LPR + sj; e < hi_r; e += LPR) {
                     const uint32_t key = __ldg(&a.row.keys[rbase + e]);
                     D[d_slot(key & wmask, rr)] = __ldg(&a.row.vals[rbase + e]);
                 }
@@ -295,7 +299,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
             for (int t = 0; t < NPF; t++)
                 if (ck[t] != 0xffffffffu) D[d_slot(ck[t] & wmask, rr)] = 0.0f;
             if (has_row) {
-                for (uint32_t e = lo_r + 32 + sj; e < hi_r; e += LPR) {
+                for (uint32_t e = lo_r + NPF * LPR + sj; e < hi_r; e += LPR) {
                     const uint32_t key = __ldg(&a.row.keys[rbase + e]);
                     D[d_slot(key & wmask, rr)] = 0.0f;
                 }

@@ -106,9 +106,10 @@ def test_batched_build_equals_single_and_counts():
         assert ulp_diff(v, r["values"]) <= 1
         assert arena.off[i] % 4 == 0
         assert abs(arena.norms[i] - r["norm"]) <= 1e-12 * r["norm"]
-    # count tables of the last plan (proteomes 4, 5)
+    # count tables of the last plan (proteomes 4, 5; the second batch, on the builder's
+    # second scratch when two batches are in flight)
     L = _native.load()
-    scr = b._scratch
+    scr = b._scratch[1] if b.overlap else b._scratch[0]
     k1 = np.zeros(21 ** 5, np.uint32)
     k2 = np.zeros(21 ** 4, np.uint32)
     tot = np.zeros(3, np.uint32)
