@@ -88,7 +88,7 @@ __device__ __forceinline__ void fold16(float (&acc)[16], float (&hi)[16], float 
 #endif
 // Row entries per lane prefetched into registers for the next window (at least).
 #ifndef AP_NPF
-#define AP_NPF 2
+#define AP_NPF 4
 #endif
 constexpr int RING = AP_RING;
 
