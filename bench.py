@@ -565,7 +565,7 @@ def main():
     ap.add_argument("--fold", type=int, default=28,
                     help="products per FP32 accumulator between compensated folds (multiple of 4)")
     ap.add_argument("--items-per-cta", type=int, default=8)
-    ap.add_argument("--max-batch", type=int, default=32)
+    ap.add_argument("--max-batch", type=int, default=24)
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-pair ABI measurement")

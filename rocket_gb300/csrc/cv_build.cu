@@ -21,7 +21,7 @@
 //   scan, k_cand_bases   candidate offsets; proteome p's candidates start at
 //                   cbase[p], a multiple of ALPHA_TILE
 //   k_cand_offsets  per-(K-1)-mer candidate offsets; the (K-1)-mer of every candidate
-//   k_c0_zero/k_c0_scatter   K-mer counts into candidate slots
+//   k_c0_scatter    K-mer counts into candidate slots (zeroed by k_cand_offsets)
 //   k_alpha         Markov alpha (reference double order) of every candidate, flat
 //                   over the candidates; each warp compacts its segment's survivors
 //                   (alpha bits and key) to the segment's start; norm partials
@@ -372,6 +372,18 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
         (uint32_t)(a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH] + ex);
     uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
     const uint64_t gb = a.cbase[p];
+    // zero this warp's candidate slots (counts and marks), coalesced: the warp's
+    // candidates are the contiguous range of its 32 words
+    {
+        const int lane = threadIdx.x & 31;
+        const uint64_t w0 = gb + __shfl_sync(0xffffffffu, run, 0);
+        const uint64_t w1 = gb + __shfl_sync(0xffffffffu, run + s, 31);
+        for (uint64_t i = w0 + lane; i < w1 && i < a.cand_cap; i += 32) {
+            a.c0a[i] = 0u;
+            a.cq[i] = 0u;
+        }
+        __syncwarp();
+    }
     // cq marks (q + 1) the first candidate of q, and the first of a segment that
     // q's run reaches into (the rest of cq is zero); k_alpha takes each
     // candidate's (K-1)-mer from the last mark at or before it.  Set bits four
@@ -414,16 +426,6 @@ __global__ void k_cand_bases(BuildArgs a) {
     a.cbase[a.B] = run;
     *a.cand_total = run;
     if (run > a.cand_cap) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
-}
-
-// zero the K-mer count slots and (K-1)-mer marks of all candidates (bounded by capacity)
-__global__ void k_c0_zero(BuildArgs a) {
-    const uint64_t total = min(*a.cand_total, a.cand_cap);  // k_cand_bases flags overflow
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        a.c0a[i] = 0;
-        a.cq[i] = 0;
-    }
 }
 
 // Every K-window adds one to the slot of its candidate (native.cu:244).
@@ -840,7 +842,6 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
     k_cand_bases<<<1, 32, 0, st>>>(a);
-    k_c0_zero<<<sm_count() * 4, 256, 0, st>>>(a);
     k_cand_offsets<<<gch, CHUNK_THREADS, 0, st>>>(a);
     k_c0_scatter<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
     const unsigned ncta = (unsigned)(a.cand_cap / ALPHA_TILE);
@@ -859,9 +860,9 @@ cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
 
 // Kernel counting per launch of build_plan + build_emit (for launch accounting).
 // Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_tables,
-// k_tuple_alpha, k_cand_count, scan (3), k_cand_bases, k_cand_offsets, k_c0_zero,
+// k_tuple_alpha, k_cand_count, scan (3), k_cand_bases, k_cand_offsets,
 // k_c0_scatter, k_alpha, scan (3), k_norm, k_tuple_value; emit
-// k_arena_offsets, k_compact, k_arena_pad.  (Five memsets are not counted.)
-int build_launches_per_batch() { return 18 + 3; }
+// k_arena_offsets, k_compact, k_arena_pad.  (Six memsets are not counted.)
+int build_launches_per_batch() { return 17 + 3; }
 
 }  // namespace phylo

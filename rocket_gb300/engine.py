@@ -127,7 +127,7 @@ class BatchBuilder:
     flight at once, on the caller's stream and a second stream with their own
     scratch, so that one batch's kernels fill the gaps of the other's."""
 
-    def __init__(self, alphabet: str = "protein", k: int = 6, device=None, max_batch: int = 32,
+    def __init__(self, alphabet: str = "protein", k: int = 6, device=None, max_batch: int = 24,
                  overlap: bool = True):
         self.alphabet = alphabet
         self.k = k
