@@ -259,7 +259,6 @@ __global__ void k_tuple_value(BuildArgs a) {
 // Counts (K-2)- and (K-1)-windows, marks right extensions, totals n0/n1/n2.
 // A window starting at i counts for length L when its L symbols are all in the
 // alphabet and inside the proteome (native.cu:236-252).
-template <bool SEEN_FROM_COUNTS>
 __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
     __shared__ uint8_t dig[TILE + 16];
     __shared__ uint32_t ntot[3];
@@ -299,16 +298,11 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             const bool v2 = run >= K - 2, v1 = run >= K - 1, v0 = run >= K;
             cnt2 += v2; cnt1 += v1; cnt0 += v0;
             // counts and extension masks: reduction atomics (equal keys within a
-            // warp are rare, so no aggregation).  Small (K-1)-mer tables get their
-            // seen bitmap from the counts afterwards (k_seen); large ones set the
-            // bit at the first sighting, from the count's old value.
+            // warp are rare, so no aggregation); the first sighting of a
+            // (K-1)-mer sets its seen bit
             if (v2) atomicAdd(&c2[w2], 1u);
             if (v1) {
-                if (SEEN_FROM_COUNTS) {
-                    atomicAdd(&c1[w1], 1u);
-                } else if (atomicAdd(&c1[w1], 1u) == 0u) {
-                    atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
-                }
+                if (atomicAdd(&c1[w1], 1u) == 0u) atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
                 atomicOr(&mk[w2], 1u << last);
             }
         }
@@ -324,29 +318,6 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
         __syncthreads();
         if (threadIdx.x < 3 && ntot[threadIdx.x]) atomicAdd(&a.tot[p * 4 + threadIdx.x], ntot[threadIdx.x]);
         __syncthreads();
-    }
-}
-
-// Seen bitmap from the (K-1)-mer counts: bit q of word q / 32 is set when
-// c1[q] != 0.  Each lane reads four counts; a warp covers 128 (K-1)-mers per
-// step, its ballots give four bitmap words.  grid = (ceil(T1s / 32768), B)
-__global__ void __launch_bounds__(256) k_seen(BuildArgs a) {
-    const int p = blockIdx.y;
-    const int lane = threadIdx.x & 31;
-    const uint64_t nq = a.T1s;
-    const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
-    uint32_t *seen = a.seen1 + (uint64_t)p * (a.T1s / 32);
-    const uint64_t base = (uint64_t)blockIdx.x * 32768 + (threadIdx.x >> 5) * 4096;
-    for (uint64_t q0 = base; q0 < base + 4096 && q0 < nq; q0 += 128) {
-        const uint64_t q = q0 + 4 * lane;
-        const uint4 c = q < nq ? *reinterpret_cast<const uint4 *>(c1 + q) : make_uint4(0, 0, 0, 0);
-        // lane l holds (K-1)-mers q0 + 4l .. q0 + 4l + 3: word j of the four covers lanes 8j..8j+7
-        const uint32_t nib = (c.x != 0u) | ((c.y != 0u) << 1) | ((c.z != 0u) << 2) | ((c.w != 0u) << 3);
-        uint32_t word = nib << (4 * (lane & 7));
-        word |= __shfl_xor_sync(0xffffffffu, word, 1);
-        word |= __shfl_xor_sync(0xffffffffu, word, 2);
-        word |= __shfl_xor_sync(0xffffffffu, word, 4);
-        if ((lane & 7) == 0 && q < nq) seen[q / 32] = word;
     }
 }
 
@@ -857,23 +828,14 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const uint64_t nc = (uint64_t)a.B * a.NCH;
     // dense tables c1 | coff | c2 | mask | tot are contiguous in scratch: zero what needs it
     PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1s * a.B, st));
-    if (a.T1s > (1ull << 24))  // otherwise k_seen writes every word
-        PHYLO_CHECK(cudaMemsetAsync(a.seen1, 0, sizeof(uint32_t) * (a.T1s / 32) * a.B, st));
+    PHYLO_CHECK(cudaMemsetAsync(a.seen1, 0, sizeof(uint32_t) * (a.T1s / 32) * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.mask, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.tot, 0, sizeof(uint32_t) * 4 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.status, 0, sizeof(uint32_t) * 4, st));
     k_prep<<<1, 32, 0, st>>>(a.B, a.seq_off, a.tile_base);
     const int grid_seq = sm_count() * 8;
-    // (K-1)-mer tables up to 2^24 entries: plain reduction atomics, then the
-    // seen bitmap from the counts (a dense pass of 4 B per (K-1)-mer)
-    const bool seen_from_counts = a.T1s <= (1ull << 24);
-    if (seen_from_counts) {
-        k_count<true><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
-        k_seen<<<dim3((unsigned)div_up(a.T1s, 32768), a.B), 256, 0, st>>>(a);
-    } else {
-        k_count<false><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
-    }
+    k_count<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
     k_tables<<<dim3(PROB_TABLE / 256, a.B), 256, 0, st>>>(a);
     k_tuple_alpha<<<dim3(TUPLE_TABLE / 256, a.B), 256, 0, st>>>(a);
     dim3 gch((unsigned)a.NCH, (unsigned)a.B);
@@ -898,9 +860,9 @@ cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
 
 // Kernel counting per launch of build_plan + build_emit (for launch accounting).
 // Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_tables,
-// k_seen, k_tuple_alpha, k_cand_count, scan (3), k_cand_bases, k_cand_offsets,
+// k_tuple_alpha, k_cand_count, scan (3), k_cand_bases, k_cand_offsets,
 // k_c0_scatter, k_alpha, scan (3), k_norm, k_tuple_value; emit
 // k_arena_offsets, k_compact, k_arena_pad.  (Six memsets are not counted.)
-int build_launches_per_batch() { return 18 + 3; }  // k_seen counted (K-1 tables <= 2^24)
+int build_launches_per_batch() { return 17 + 3; }
 
 }  // namespace phylo
