@@ -20,7 +20,7 @@
 //   k_cand_count    candidates per chunk of 2048 (K-1)-mers
 //   scan, k_cand_bases   candidate offsets; proteome p's candidates start at
 //                   cbase[p], a multiple of ALPHA_TILE
-//   k_cand_offsets  per-(K-1)-mer candidate offsets; the (K-1)-mer of every candidate
+//   k_cand_offsets  per-(K-1)-mer candidate offsets; the key of every candidate
 //   k_c0_scatter    K-mer counts into candidate slots (zeroed by k_cand_offsets)
 //   k_alpha         Markov alpha (reference double order) of every candidate, flat
 //                   over the candidates; each warp compacts its segment's survivors
@@ -353,12 +353,20 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     }
 }
 
+// Keys staged per warp in shared memory before the coalesced store.
+constexpr uint32_t KEY_STAGE = 2048;
+
 // coff[p][q] = candidate offset of seen (K-1)-mer q within proteome p (entries
-// of unseen q are not written); head marks of the (K-1)-mers in cq.
-// grid = (NCH, B)
+// of unseen q are not written); cq = the key q * A + b of every candidate (b
+// over the right-extension mask of q's suffix, ascending), c0a zeroed.  A warp's
+// candidates are the contiguous range of its 32 bitmap words: their keys are
+// assembled in shared memory and stored coalesced (a range larger than the
+// stage is written directly).  grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
+    __shared__ uint32_t stage[CHUNK_THREADS / 32][KEY_STAGE];
     const int p = blockIdx.y, c = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
     const uint64_t nw = a.T1s / 32;
     const uint64_t wd = (uint64_t)c * CHUNK_THREADS + threadIdx.x;
@@ -372,43 +380,45 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
         (uint32_t)(a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH] + ex);
     uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
     const uint64_t gb = a.cbase[p];
-    // zero this warp's candidate slots (counts and marks), coalesced: the warp's
-    // candidates are the contiguous range of its 32 words
-    {
-        const int lane = threadIdx.x & 31;
-        const uint64_t w0 = gb + __shfl_sync(0xffffffffu, run, 0);
-        const uint64_t w1 = gb + __shfl_sync(0xffffffffu, run + s, 31);
-        for (uint64_t i = w0 + lane; i < w1 && i < a.cand_cap; i += 32) {
-            a.c0a[i] = 0u;
-            a.cq[i] = 0u;
-        }
-        __syncwarp();
-    }
-    // cq marks (q + 1) the first candidate of q, and the first of a segment that
-    // q's run reaches into (the rest of cq is zero); k_alpha takes each
-    // candidate's (K-1)-mer from the last mark at or before it.  Set bits four
-    // at a time, so that their mask loads are in flight together.
+    const uint32_t r0 = __shfl_sync(0xffffffffu, run, 0);
+    const uint32_t r1 = __shfl_sync(0xffffffffu, run + s, 31);
+    const uint64_t w0 = gb + r0, w1 = gb + r1;
+    const bool staged = r1 - r0 <= KEY_STAGE;
+    // zero this warp's K-mer count slots (coalesced)
+    for (uint64_t i = w0 + lane; i < w1 && i < a.cand_cap; i += 32) a.c0a[i] = 0u;
+    // this lane's candidates: seen q in ascending order, then b ascending
+    const uint32_t A = a.A;
     uint32_t rest = bits;
     while (rest) {
-        uint32_t qs[4], ns[4];
+        uint32_t qs[4], ms[4];
 #pragma unroll
         for (int t = 0; t < 4; t++) {
             qs[t] = rest ? q0 + (uint32_t)(__ffs(rest) - 1) : 0xffffffffu;
             rest &= rest - 1;
-            ns[t] = qs[t] != 0xffffffffu ? (uint32_t)__popc(__ldg(&mk[a.fdT2.mod(qs[t])])) : 0u;
+            ms[t] = qs[t] != 0xffffffffu ? __ldg(&mk[a.fdT2.mod(qs[t])]) : 0u;
         }
 #pragma unroll
         for (int t = 0; t < 4; t++) {
             if (qs[t] == 0xffffffffu) break;
-            const uint32_t q = qs[t], n = ns[t];
-            coff[q] = run;
-            if (n == 0) continue;  // no candidate: its offset is the next one's
-            const uint64_t g = gb + run;
-            if (g < a.cand_cap) a.cq[g] = q + 1u;
-            const uint64_t nb = (g / SEG + 1) * SEG;
-            if (nb < g + n && nb < a.cand_cap) a.cq[nb] = q + 1u;
-            run += n;
+            const uint32_t q = qs[t];
+            coff[q] = run;  // no candidate: its offset is the next one's
+            uint32_t e = ms[t];
+            while (e) {
+                const uint32_t key = q * A + (uint32_t)(__ffs(e) - 1);
+                e &= e - 1;
+                if (staged) {
+                    stage[warp][run - r0] = key;
+                } else if (gb + run < a.cand_cap) {
+                    a.cq[gb + run] = key;
+                }
+                run++;
+            }
         }
+    }
+    if (staged) {
+        __syncwarp();
+        for (uint32_t i = lane; i < r1 - r0; i += 32)
+            if (w0 + i < a.cand_cap) a.cq[w0 + i] = stage[warp][i];
     }
 }
 
@@ -500,10 +510,8 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     const int p = find_owner(a.cbase, a.B, g0);
     const uint32_t np =
         (uint32_t)(a.chunk_cand_off[(uint64_t)(p + 1) * a.NCH] - a.chunk_cand_off[(uint64_t)p * a.NCH]);
-    const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
     const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
     const uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
-    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
     const double *prob = a.prob + (uint64_t)p * 4 * PROB_TABLE;
     const uint32_t *atab = a.atab + (uint64_t)p * TUPLE_TABLE;
     const uint32_t n0 = a.tot[p * 4 + 0], n1 = a.tot[p * 4 + 1], n2 = a.tot[p * 4 + 2];
@@ -513,52 +521,36 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
     U192 acc = {0, 0, 0};
     uint32_t m1 = 0, bad = 0, nsurv = 0;
     constexpr int NI = SEG / 32;  // candidates per lane
-    // phase 1: marks and counts of the whole segment, then the (K-1)-mer of
-    // each candidate = the last mark at or before it (marks ascend along the
-    // candidates; every segment starts with one)
-    uint32_t q[NI], full[NI];
+    // phase 1: keys and K-mer counts of the whole segment
+    uint32_t kk[NI], full[NI];
 #pragma unroll
     for (int i = 0; i < NI; i++) {
         const uint32_t ul = loc0 + 32 * i + lane;
         const uint64_t u = sbase + 32 * i + lane;
-        q[i] = ul < np ? a.cq[u] : 0u;
+        kk[i] = ul < np ? a.cq[u] : 0u;
         full[i] = ul < np ? a.c0a[u] : 0u;
     }
-    uint32_t carry = 0;
-    const uint32_t le = 0xffffffffu >> (31 - lane);  // lanes at or below this one
-#pragma unroll
-    for (int i = 0; i < NI; i++) {
-        const uint32_t marks = __ballot_sync(0xffffffffu, q[i] != 0u) & le;
-        const uint32_t v = __shfl_sync(0xffffffffu, q[i], marks ? 31 - __clz(marks) : 0);
-        q[i] = marks ? v - 1u : carry;
-        carry = __shfl_sync(0xffffffffu, q[i], 31);
-    }
-    // phase 2: alpha, four candidates per lane at a time (their table loads in flight together)
+    // phase 2: alpha, four candidates per lane at a time (their table loads in flight
+    // together); an unseen K-mer (count 0) has alpha -1 and needs no count loads
 #pragma unroll
     for (int h = 0; h < NI; h += 4) {
-        uint32_t mm[4], mkv[4], co[4], pre[4], mid[4], b[4], suf[4];
+        uint32_t qq[4], mm[4], bb[4], pre[4], mid[4], suf[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            mm[j] = a.fdT2.mod(q[h + j]);
-            const bool ok = loc0 + 32 * (h + j) + lane < np;
-            const bool seen = ok && full[h + j] != 0u;  // an unseen K-mer's alpha is -1
-            mkv[j] = ok ? __ldg(&mk[mm[j]]) : 0u;
-            co[j] = ok ? __ldg(&coff[q[h + j]]) : 0u;
-            pre[j] = seen ? __ldg(&c1[q[h + j]]) : 0u;
+            const uint32_t key = kk[h + j];
+            qq[j] = A == 21u ? key / 21u : key >> 2;  // protein or DNA alphabet
+            bb[j] = key - qq[j] * A;
+            mm[j] = a.fdT2.mod(qq[j]);
+            const bool seen = loc0 + 32 * (h + j) + lane < np && full[h + j] != 0u;
+            pre[j] = seen ? __ldg(&c1[qq[j]]) : 0u;
             mid[j] = seen ? __ldg(&c2[mm[j]]) : 0u;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const uint32_t ul = loc0 + 32 * (h + j) + lane;
-            const bool ok = ul < np;
-            b[j] = ok ? nth_set_bit(mkv[j], ul - co[j]) : 0u;
-            suf[j] = ok && full[h + j] != 0u ? __ldg(&c1[mm[j] * A + b[j]]) : 0u;
+            suf[j] = seen ? __ldg(&c1[mm[j] * A + bb[j]]) : 0u;
         }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const int i = h + j;
             const bool ok = loc0 + 32 * i + lane < np;
-            uint32_t stored = 0, key = 0;
+            uint32_t stored = 0;
             float f = 0.0f;
             if (ok) {
                 if (full[i] - 1u < 3u && pre[j] < (uint32_t)TUPLE_PS &&
@@ -572,7 +564,6 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
                     f = markov_alpha_fast(full[i], pre[j], suf[j], mid[j], n0, n1, n2, prob);
                     stored = __float_as_uint(f);
                 }
-                key = q[i] * A + b[j];
             }
             const bool surv = __float_as_uint(f) != 0u;
             const unsigned bal = __ballot_sync(0xffffffffu, surv);
@@ -580,7 +571,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
                 // positions at or before this lane's own: already read (phase 1)
                 const uint64_t pos = sbase + nsurv + __popc(bal & ((1u << lane) - 1u));
                 a.c0a[pos] = stored;
-                a.cq[pos] = key;
+                a.cq[pos] = kk[i];
                 const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
                 if (sq == 1.0f) m1++;
                 else if (isnan(sq)) bad |= 1u;

@@ -12,17 +12,20 @@ struct BuildGeometry {
     uint64_t NCH;    // chunks of (K-1)-mers per proteome
 };
 
-// Division by a run-time constant d (2 <= d < 2^32) for 32-bit numerators:
-// q / d == floor(q * M / 2^64) with M = ceil(2^64 / d).
+// Remainder by a run-time constant d (4 <= d < 2^31) for 32-bit numerators:
+// with R = ceil(2^32 / d), a = floor(q * R / 2^32) is floor(q / d) or one more
+// (q * R / 2^32 exceeds q / d by less than q / 2^32 < 1), so q - a * d is the
+// remainder, or the remainder - d, corrected by one conditional add.
 struct FastDiv {
-    uint64_t M;
-    uint32_t d;
+    uint32_t R, d;
     __host__ void set(uint32_t divisor) {
         d = divisor;
-        M = ~0ull / divisor + 1;  // ceil(2^64 / d) for d not a power of two; exact otherwise
+        R = (uint32_t)((0xffffffffull + divisor) / divisor);  // ceil(2^32 / d)
     }
-    __device__ __forceinline__ uint32_t div(uint32_t q) const { return (uint32_t)__umul64hi(q, M); }
-    __device__ __forceinline__ uint32_t mod(uint32_t q) const { return q - div(q) * d; }
+    __device__ __forceinline__ uint32_t mod(uint32_t q) const {
+        const uint32_t r = q - __umulhi(q, R) * d;
+        return (int32_t)r < 0 ? r + d : r;
+    }
 };
 
 // Candidates per k_alpha CTA (proteomes start on multiples of it) and per
@@ -65,7 +68,7 @@ struct BuildArgs {
     // multiple of ALPHA_TILE; cbase[B] = *cand_total
     uint64_t *cbase;          // [B+1]
     uint64_t *cand_total;     // [1]
-    uint32_t *cq;             // [cand_cap]: (K-1)-mer marks (q + 1), then the key of each survivor
+    uint32_t *cq;             // [cand_cap]: the key of each candidate, then of each survivor
     // per segment of SEG candidates (survivors compacted to the segment's start)
     uint32_t *seg_surv;       // [nseg]
     uint64_t *seg_out_off;    // exclusive scan, [nseg+1]
