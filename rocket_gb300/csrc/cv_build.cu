@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
 // (alpha bits != 0) are compacted, in key order, to the start of their segment:
 // c0a holds their alpha bits (or TUPLE_TAG | tuple), cq their keys; seg_surv the
 // count.  Per-CTA norm partials.  grid = cand_cap / ALPHA_TILE
-__global__ void __launch_bounds__(CHUNK_THREADS) k_alpha(BuildArgs a) {
+__global__ void __launch_bounds__(CHUNK_THREADS, 3) k_alpha(BuildArgs a) {
     __shared__ U192 s_norm[CHUNK_THREADS / 32];
     __shared__ uint32_t s_m1[CHUNK_THREADS / 32], s_bad[CHUNK_THREADS / 32];
     const uint64_t c = blockIdx.x;
