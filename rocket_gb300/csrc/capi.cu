@@ -378,6 +378,7 @@ int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_si
     memset(&a, 0, sizeof(a));
     PHYLO_CHECK(build_carve(g, num_proteomes, (uint64_t)max_candidates, (void *)d_scratch,
                             (size_t)scratch_size, &a));
+    if (a.compact1) return (int)cudaErrorNotSupported;  // no dense (K-1)-mer rows to copy
     cudaStream_t st = (cudaStream_t)stream;
     PHYLO_CHECK(cudaMemcpyAsync(h_c1, a.c1 + (uint64_t)p * g.T1s, sizeof(uint32_t) * g.T1,
                                 cudaMemcpyDeviceToHost, st));

@@ -30,6 +30,7 @@
 //   (host reads nnz, checks capacity)
 //   k_compact       survivors' keys and normalised values, copied segment by segment
 #include "cv_build.cuh"
+#include "rank.cuh"
 #include "scan.cuh"
 
 namespace phylo {
@@ -185,6 +186,15 @@ __device__ double u192_to_double(const U192 &a) {
     return ldexp((double)mant, pos - 52 - 96);
 }
 
+// Index of (K-1)-mer q of proteome p in the c1 / coff tables: q itself (dense
+// rows of T1s entries), or its rank among the batch's seen (K-1)-mers (compact).
+__device__ __forceinline__ uint64_t c1_index(const BuildArgs &a, int p, uint32_t q) {
+    if (!a.compact1) return (uint64_t)p * a.T1s + q;
+    const uint64_t w = (uint64_t)p * (a.T1s / 32) + (q >> 5);
+    return (uint64_t)__ldg(&a.prefix1[w]) +
+           (uint32_t)__popc(__ldg(&a.seen1[w]) & ((1u << (q & 31u)) - 1u));
+}
+
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
@@ -259,6 +269,7 @@ __global__ void k_tuple_value(BuildArgs a) {
 // Counts (K-2)- and (K-1)-windows, marks right extensions, totals n0/n1/n2.
 // A window starting at i counts for length L when its L symbols are all in the
 // alphabet and inside the proteome (native.cu:236-252).
+template <bool COMPACT>
 __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
     __shared__ uint8_t dig[TILE + 16];
     __shared__ uint32_t ntot[3];
@@ -275,7 +286,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             dig[j] = pos < len ? (uint8_t)char_to_digit(a.alpha, a.seq[s0 + pos]) : (uint8_t)0xff;
         }
         __syncthreads();
-        uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
+        uint32_t *c1 = COMPACT ? nullptr : a.c1 + (uint64_t)p * a.T1s;
         uint32_t *seen = a.seen1 + (uint64_t)p * (a.T1s / 32);
         uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
         uint32_t *mk = a.mask + (uint64_t)p * a.T2;
@@ -300,9 +311,15 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             // counts and extension masks: reduction atomics (equal keys within a
             // warp are rare, so no aggregation); the first sighting of a
             // (K-1)-mer sets its seen bit
+            // (compact tables: only the seen bit here; k_c0_scatter counts once the
+            // ranks of the seen (K-1)-mers are known)
             if (v2) atomicAdd(&c2[w2], 1u);
             if (v1) {
-                if (atomicAdd(&c1[w1], 1u) == 0u) atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                if (COMPACT) {
+                    atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                } else if (atomicAdd(&c1[w1], 1u) == 0u) {
+                    atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                }
                 atomicOr(&mk[w2], 1u << last);
             }
         }
@@ -378,7 +395,6 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     const uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
     uint32_t run =
         (uint32_t)(a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH] + ex);
-    uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
     const uint64_t gb = a.cbase[p];
     const uint32_t r0 = __shfl_sync(0xffffffffu, run, 0);
     const uint32_t r1 = __shfl_sync(0xffffffffu, run + s, 31);
@@ -401,7 +417,11 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
         for (int t = 0; t < 4; t++) {
             if (qs[t] == 0xffffffffu) break;
             const uint32_t q = qs[t];
-            coff[q] = run;  // no candidate: its offset is the next one's
+            const uint64_t qi = c1_index(a, p, q);
+            if (!a.compact1 || qi < a.cap1) {
+                a.coff[qi] = run;  // no candidate: its offset is the next one's
+                if (a.compact1) a.c1[qi] = 0u;  // counted by k_c0_scatter
+            }
             uint32_t e = ms[t];
             while (e) {
                 const uint32_t key = q * A + (uint32_t)(__ffs(e) - 1);
@@ -436,9 +456,11 @@ __global__ void k_cand_bases(BuildArgs a) {
     a.cbase[a.B] = run;
     *a.cand_total = run;
     if (run > a.cand_cap) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
+    if (a.compact1 && *a.p1_total > a.cap1) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
 }
 
-// Every K-window adds one to the slot of its candidate (native.cu:244).
+// Every K-window adds one to the slot of its candidate (native.cu:244); with
+// compact (K-1)-mer tables every (K-1)-window also adds one to its count.
 __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
     __shared__ uint8_t dig[TILE + 16];
     const int K = a.k;
@@ -453,7 +475,6 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
             dig[j] = pos < len ? (uint8_t)char_to_digit(a.alpha, a.seq[s0 + pos]) : (uint8_t)0xff;
         }
         __syncthreads();
-        const uint32_t *coff = a.coff + (uint64_t)p * a.T1s;
         const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         const uint64_t cbase = a.cbase[p];
         for (int u = 0; u < TILE / COUNT_THREADS; u++) {
@@ -469,11 +490,14 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
                     w = w * A + d;
                 }
                 if (j == K - 1) {
+                    const uint64_t wi = c1_index(a, p, w);
+                    const bool in_cap = !a.compact1 || wi < a.cap1;
+                    if (a.compact1 && in_cap) atomicAdd(&a.c1[wi], 1u);  // (K-1)-window count
                     uint32_t b = dig[li + K - 1];
-                    if (b != 0xffu) {
+                    if (b != 0xffu && in_cap) {
                         v0 = true;
                         uint32_t m = a.fdT2.mod(w);
-                        slot = cbase + coff[w] + __popc(mk[m] & ((1u << b) - 1u));
+                        slot = cbase + a.coff[wi] + __popc(mk[m] & ((1u << b) - 1u));
                     }
                 }
             }
@@ -510,7 +534,6 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 3) k_alpha(BuildArgs a) {
     const int p = find_owner(a.cbase, a.B, g0);
     const uint32_t np =
         (uint32_t)(a.chunk_cand_off[(uint64_t)(p + 1) * a.NCH] - a.chunk_cand_off[(uint64_t)p * a.NCH]);
-    const uint32_t *c1 = a.c1 + (uint64_t)p * a.T1s;
     const uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
     const double *prob = a.prob + (uint64_t)p * 4 * PROB_TABLE;
     const uint32_t *atab = a.atab + (uint64_t)p * TUPLE_TABLE;
@@ -542,9 +565,9 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 3) k_alpha(BuildArgs a) {
             bb[j] = key - qq[j] * A;
             mm[j] = a.fdT2.mod(qq[j]);
             const bool seen = loc0 + 32 * (h + j) + lane < np && full[h + j] != 0u;
-            pre[j] = seen ? __ldg(&c1[qq[j]]) : 0u;
+            pre[j] = seen ? __ldg(&a.c1[c1_index(a, p, qq[j])]) : 0u;
             mid[j] = seen ? __ldg(&c2[mm[j]]) : 0u;
-            suf[j] = seen ? __ldg(&c1[mm[j] * A + bb[j]]) : 0u;
+            suf[j] = seen ? __ldg(&a.c1[c1_index(a, p, mm[j] * A + bb[j])]) : 0u;
         }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
@@ -711,6 +734,10 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     return 0;
 }
 
+// (K-1)-mer tables beyond 2^24 entries per proteome (protein K = 7) are kept
+// compact: one entry per seen (K-1)-mer instead of a dense row.
+static bool compact1_tables(const BuildGeometry &g) { return g.T1s > (1ull << 24); }
+
 // Candidate capacity rounded up to whole k_alpha CTAs.
 static uint64_t cand_cap_rounded(uint64_t cand_cap) {
     return div_up(cand_cap ? cand_cap : 1, (uint64_t)ALPHA_TILE) * ALPHA_TILE;
@@ -721,8 +748,14 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     const uint64_t cap = cand_cap_rounded(cand_cap);
     const uint64_t ncta = cap / ALPHA_TILE, nseg = cap / SEG;
     size_t s = 0;
-    s += scratch_bytes<uint32_t>(g.T1s * B);       // c1 (rows padded to 8 entries)
-    s += scratch_bytes<uint32_t>(g.T1s * B);       // coff
+    const bool compact = compact1_tables(g);
+    const uint64_t n1 = compact ? cap : g.T1s * B;  // entries of c1 / coff
+    const uint64_t nw1 = g.T1s / 32 * B;
+    s += scratch_bytes<uint32_t>(n1);              // c1
+    s += scratch_bytes<uint32_t>(n1);              // coff
+    s += scratch_bytes<uint32_t>(compact ? nw1 : 0);                        // prefix1
+    s += scratch_bytes<uint64_t>(compact ? bitmap_prefix_partials(nw1) : 0);  // p1_partials
+    s += scratch_bytes<uint64_t>(1);               // p1_total
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // seen1
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // word_cand
     s += scratch_bytes<uint32_t>(g.T2 * B);        // c2
@@ -765,8 +798,16 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     BuildArgs &r = *a;
     r.alpha = g.alpha; r.k = g.k; r.A = g.A; r.T1 = g.T1; r.T2 = g.T2; r.NCH = g.NCH; r.B = B;
     r.T1s = g.T1s;
-    r.c1 = sc.take<uint32_t>(g.T1s * B);
-    r.coff = sc.take<uint32_t>(g.T1s * B);
+    const bool compact = compact1_tables(g);
+    const uint64_t n1 = compact ? cap : g.T1s * B;
+    const uint64_t nw1 = g.T1s / 32 * B;
+    r.compact1 = compact ? 1 : 0;
+    r.cap1 = n1;
+    r.c1 = sc.take<uint32_t>(n1);
+    r.coff = sc.take<uint32_t>(n1);
+    r.prefix1 = sc.take<uint32_t>(compact ? nw1 : 0);
+    r.p1_partials = sc.take<uint64_t>(compact ? bitmap_prefix_partials(nw1) : 0);
+    r.p1_total = sc.take<uint64_t>(1);
     r.seen1 = sc.take<uint32_t>(g.T1s / 32 * B);
     r.word_cand = sc.take<uint32_t>(g.T1s / 32 * B);
     r.c2 = sc.take<uint32_t>(g.T2 * B);
@@ -818,7 +859,7 @@ static int sm_count() {
 cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const uint64_t nc = (uint64_t)a.B * a.NCH;
     // dense tables c1 | coff | c2 | mask | tot are contiguous in scratch: zero what needs it
-    PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1s * a.B, st));
+    if (!a.compact1) PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1s * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.seen1, 0, sizeof(uint32_t) * (a.T1s / 32) * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.mask, 0, sizeof(uint32_t) * a.T2 * a.B, st));
@@ -826,7 +867,14 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     PHYLO_CHECK(cudaMemsetAsync(a.status, 0, sizeof(uint32_t) * 4, st));
     k_prep<<<1, 32, 0, st>>>(a.B, a.seq_off, a.tile_base);
     const int grid_seq = sm_count() * 8;
-    k_count<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
+    if (a.compact1) {
+        k_count<true><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
+        PHYLO_CHECK(bitmap_prefix(a.seen1, a.T1s / 32 * a.B, a.p1_partials, a.prefix1,
+                                  a.p1_total, st));
+    } else {
+        k_count<false><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
+        PHYLO_CHECK(cudaMemsetAsync(a.p1_total, 0, sizeof(uint64_t), st));
+    }
     k_tables<<<dim3(PROB_TABLE / 256, a.B), 256, 0, st>>>(a);
     k_tuple_alpha<<<dim3(TUPLE_TABLE / 256, a.B), 256, 0, st>>>(a);
     dim3 gch((unsigned)a.NCH, (unsigned)a.B);

@@ -100,6 +100,17 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_apply(const uint32_t *__res
     }
 }
 
+cudaError_t bitmap_prefix(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
+                          uint32_t *prefix, uint64_t *total, cudaStream_t st) {
+    const uint64_t nb = div_up(nwords ? nwords : 1, SCAN_TILE);
+    k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials);
+    k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
+    k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials, prefix, total);
+    return cudaGetLastError();
+}
+
+uint64_t bitmap_prefix_partials(uint64_t nwords) { return div_up(nwords ? nwords : 1, SCAN_TILE) + 1; }
+
 static uint64_t rank_words(uint64_t key_limit) { return div_up(key_limit ? key_limit : 1, 32); }
 
 size_t rank_bitmap_words(uint64_t key_limit) { return rank_words(key_limit); }

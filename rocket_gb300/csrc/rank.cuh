@@ -20,4 +20,11 @@ cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
 
 int key_ranks_launches(bool marked);
 
+// prefix[w] = set bits of words [0, w) of a bitmap (uint32 counts; the total
+// must stay below 2^32), *total = all set bits (device).  partials holds
+// bitmap_prefix_partials(nwords) entries.  Three launches.
+cudaError_t bitmap_prefix(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
+                          uint32_t *prefix, uint64_t *total, cudaStream_t st);
+uint64_t bitmap_prefix_partials(uint64_t nwords);
+
 }  // namespace phylo

@@ -36,7 +36,7 @@ def test_known_answers(seq, k, expect):
         assert n == expect
 
 
-@pytest.mark.parametrize("k", [3, 4, 5, 6])
+@pytest.mark.parametrize("k", [3, 4, 5, 6, 7])
 def test_bindings_sweep_protein(k):
     # the sweep of BindingsTest.testBuildVectors (n x seeds, :99-112)
     for n in (10, 100, 1000, 10000):
@@ -59,6 +59,20 @@ def test_dna_k10():
 def test_synthetic_proteome(k):
     p = synth.workload("uniform256", n=2, scale=0.2)
     check_against_oracle(p.get(1), k)
+
+
+def test_batched_build_k7_compact_tables():
+    """Protein K = 7: (K-1)-mer tables of 21^6 entries are kept compact (one entry per
+    seen (K-1)-mer); two batches, keys and values against the oracle."""
+    p = synth.workload("uneven1024", n=5, scale=0.05)
+    d = torch.from_numpy(p.data).cuda()
+    arena = BatchBuilder("protein", 7, max_batch=3).build(d, p.offsets)
+    torch.cuda.synchronize()
+    for i in range(5):
+        r = O.cv_native(p.get(i), 7)
+        k, v = arena.host_vector(i)
+        assert np.array_equal(k, r["keys"])
+        assert ulp_diff(v, r["values"]) <= 1
 
 
 def test_full_size_proteome_k6():
