@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
 }
 
 // Keys staged per warp in shared memory before the coalesced store.
-constexpr uint32_t KEY_STAGE = 2048;
+constexpr uint32_t KEY_STAGE = 1024;
 
 // coff[p][q] = candidate offset of seen (K-1)-mer q within proteome p (entries
 // of unseen q are not written); cq = the key q * A + b of every candidate (b
