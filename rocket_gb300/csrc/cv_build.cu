@@ -39,7 +39,6 @@ constexpr int TILE = 512;            // sequence positions per counting tile (fe
                                      // proteomes' tables in flight -> L2 hits)
 constexpr int COUNT_THREADS = 256;
 constexpr int CHUNK_THREADS = 256;
-constexpr int CH = CHUNK_THREADS * 32;  // (K-1)-mers per chunk: one bitmap word per thread
 
 // ---------------------------------------------------------------------------
 // helpers
@@ -351,14 +350,23 @@ __device__ __forceinline__ uint32_t word_candidates(const BuildArgs &a, const ui
     return s;
 }
 
-// Candidates per chunk of CH (K-1)-mers.  grid = (NCH, B)
+// Candidates per chunk of CHUNK_THREADS * wpt bitmap words (wpt consecutive
+// words per thread: 4 for the sparse bitmaps of compact (K-1)-mer tables, else 1).
+// grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     const int p = blockIdx.y, c = blockIdx.x;
     const uint64_t nw = a.T1s / 32;
-    const uint64_t wd = (uint64_t)c * CHUNK_THREADS + threadIdx.x;
-    const uint32_t bits = wd < nw ? a.seen1[(uint64_t)p * nw + wd] : 0u;
-    uint32_t s = word_candidates(a, a.mask + (uint64_t)p * a.T2, (uint32_t)(wd * 32), bits);
-    if (wd < nw) a.word_cand[(uint64_t)p * nw + wd] = s;
+    const uint64_t wd0 = ((uint64_t)c * CHUNK_THREADS + threadIdx.x) * a.wpt;
+    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
+    uint32_t s = 0;
+    for (uint32_t i = 0; i < a.wpt; i++) {
+        const uint64_t wd = wd0 + i;
+        if (wd >= nw) break;
+        const uint32_t bits = a.seen1[(uint64_t)p * nw + wd];
+        const uint32_t sw = bits ? word_candidates(a, mk, (uint32_t)(wd * 32), bits) : 0u;
+        a.word_cand[(uint64_t)p * nw + wd] = sw;
+        s += sw;
+    }
     s = __reduce_add_sync(0xffffffffu, s);
     __shared__ uint32_t ws[CHUNK_THREADS / 32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -371,7 +379,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
 }
 
 // Keys staged per warp in shared memory before the coalesced store.
-constexpr uint32_t KEY_STAGE = 1024;
+constexpr uint32_t KEY_STAGE = 2048;
 
 // coff[p][q] = candidate offset of seen (K-1)-mer q within proteome p (entries
 // of unseen q are not written); cq = the key q * A + b of every candidate (b
@@ -386,11 +394,10 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
     const uint64_t nw = a.T1s / 32;
-    const uint64_t wd = (uint64_t)c * CHUNK_THREADS + threadIdx.x;
-    const uint32_t q0 = (uint32_t)(wd * 32);
-    const uint32_t bits = wd < nw ? a.seen1[(uint64_t)p * nw + wd] : 0u;
+    const uint64_t wd0 = ((uint64_t)c * CHUNK_THREADS + threadIdx.x) * a.wpt;
     const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
-    const uint32_t s = wd < nw ? a.word_cand[(uint64_t)p * nw + wd] : 0u;
+    uint32_t s = 0;
+    for (uint32_t i = 0; i < a.wpt && wd0 + i < nw; i++) s += a.word_cand[(uint64_t)p * nw + wd0 + i];
     uint64_t tot;
     const uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
     uint32_t run =
@@ -404,7 +411,11 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     for (uint64_t i = w0 + lane; i < w1 && i < a.cand_cap; i += 32) a.c0a[i] = 0u;
     // this lane's candidates: seen q in ascending order, then b ascending
     const uint32_t A = a.A;
-    uint32_t rest = bits;
+    for (uint32_t wi = 0; wi < a.wpt && wd0 + wi < nw; wi++) {
+    const uint32_t q0 = (uint32_t)((wd0 + wi) * 32);
+    // (every seen (K-1)-mer, also one without candidates: its compact count slot
+    // is zeroed here, and it may be a candidate's suffix)
+    uint32_t rest = a.seen1[(uint64_t)p * nw + wd0 + wi];
     while (rest) {
         uint32_t qs[4], ms[4];
 #pragma unroll
@@ -434,6 +445,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
                 run++;
             }
         }
+    }
     }
     if (staged) {
         __syncwarp();
@@ -730,7 +742,8 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     g->T1 = ipow64(A, k - 1);
     g->T1s = (g->T1 + 31) / 32 * 32;  // whole words of the seen bitmap
     g->T2 = ipow64(A, k - 2);
-    g->NCH = div_up(g->T1, CH);
+    g->wpt = g->T1s > (1ull << 24) ? 4 : 1;  // sparse bitmaps: four words per thread
+    g->NCH = div_up(g->T1s / 32, (uint64_t)CHUNK_THREADS * g->wpt);
     return 0;
 }
 
@@ -797,6 +810,7 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     const uint64_t ncta = cap / ALPHA_TILE, nseg = cap / SEG;
     BuildArgs &r = *a;
     r.alpha = g.alpha; r.k = g.k; r.A = g.A; r.T1 = g.T1; r.T2 = g.T2; r.NCH = g.NCH; r.B = B;
+    r.wpt = g.wpt;
     r.T1s = g.T1s;
     const bool compact = compact1_tables(g);
     const uint64_t n1 = compact ? cap : g.T1s * B;

@@ -9,7 +9,8 @@ struct BuildGeometry {
     uint32_t A;      // alphabet size (21 protein, 4 DNA)
     uint64_t T1, T2; // A^(K-1), A^(K-2)
     uint64_t T1s;    // per-proteome row length of the (K-1)-mer tables (T1 rounded up to 32)
-    uint64_t NCH;    // chunks of (K-1)-mers per proteome
+    uint64_t NCH;    // chunks of the seen bitmap per proteome (CHUNK_THREADS * wpt words)
+    uint32_t wpt;    // bitmap words per thread in the candidate passes
 };
 
 // Remainder by a run-time constant d (4 <= d < 2^31) for 32-bit numerators:
@@ -50,6 +51,7 @@ struct BuildArgs {
     int alpha, k, B;
     uint32_t A;
     uint64_t T1, T2, T1s, NCH;
+    uint32_t wpt;
     // input: concatenated sequences, seq_off[B+1] (device)
     const uint8_t *seq;
     const uint64_t *seq_off;
