@@ -158,7 +158,9 @@ int phyloBuildLaunchesPerBatch(void);
 
 /* Window index of an arena: d_roff uint32[num_vectors][num_windows + 1],
  * entry [v][r] = number of entries of vector v with key < r << window_shift.
- * max_vector_len bounds the (padded) length of every vector. */
+ * max_vector_len bounds the (padded) length of every vector; every vector
+ * starts on a 4-entry (16-byte) boundary and is padded to a multiple of 4
+ * entries with keys 0xFFFFFFFF (the arena layout of phyloBuildBatchEmit). */
 int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors,
                      int window_shift, unsigned int num_windows, long max_vector_len,
                      uintptr_t d_roff);

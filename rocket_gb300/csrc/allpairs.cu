@@ -635,16 +635,20 @@ cudaError_t ap_launch(const ApArgs &a, int tile_rows, int tile_cols, int grid, c
 // window index
 // ---------------------------------------------------------------------------
 
-constexpr uint32_t RI_SLICE = 16384;  // entries per CTA
 
 // grid = (slices, N): CTA (s, v) handles entries [s*RI_SLICE, (s+1)*RI_SLICE) of
-// vector v.  Window r gets the index of the first entry whose key is >= r << wshift;
-// the CTA holding the last real entry fills the windows after it.
-__global__ void k_range_index(const uint32_t *__restrict__ keys, const uint64_t *__restrict__ vec_off,
-                              uint32_t R, uint32_t wshift, uint32_t *roff) {
+// vector v, each thread RI_RUN consecutive entries (16-byte loads; the entry before
+// a run comes from the neighbouring lane).  Window r gets the index of the first
+// entry whose key is >= r << wshift; the thread holding the last real entry fills
+// the windows after it.
+constexpr uint32_t RI_RUN = 16;
+constexpr uint32_t RI_SLICE = 256 * RI_RUN;  // entries per CTA
+__global__ void __launch_bounds__(256) k_range_index(const uint32_t *__restrict__ keys,
+                                                     const uint64_t *__restrict__ vec_off,
+                                                     uint32_t R, uint32_t wshift, uint32_t *roff) {
     const uint32_t v = blockIdx.y;
     const uint64_t b = vec_off[v];
-    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);  // padded length
+    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);  // padded length, a multiple of 4
     uint32_t *ro = roff + (uint64_t)v * (R + 1);
     const uint32_t e0 = blockIdx.x * RI_SLICE;
     if (e0 >= n) {
@@ -652,17 +656,35 @@ __global__ void k_range_index(const uint32_t *__restrict__ keys, const uint64_t 
             for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
         return;
     }
-    const uint32_t e1 = min(n, e0 + RI_SLICE);
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const uint32_t key = keys[b + e];
-        if (key == 0xffffffffu) continue;  // padding
-        const uint32_t rt = min(key >> wshift, R);
-        const int64_t rp = e == 0 ? -1 : (int64_t)min(keys[b + e - 1] >> wshift, R);
-        for (int64_t r = rp + 1; r <= (int64_t)rt; r++) ro[r] = e;
-        // last real entry: the next key is padding or the end
-        const bool last = (e + 1 == n) || keys[b + e + 1] == 0xffffffffu;
-        if (last)
-            for (uint32_t r = rt + 1; r <= R; r++) ro[r] = e + 1;
+    const int lane = threadIdx.x & 31;
+    const uint32_t s0 = e0 + threadIdx.x * RI_RUN;  // this thread's run
+    uint32_t k[RI_RUN];
+#pragma unroll
+    for (int j = 0; j < (int)RI_RUN; j += 4) {
+        uint4 q = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+        if (s0 + j < n) q = *reinterpret_cast<const uint4 *>(keys + b + s0 + j);
+        k[j] = q.x; k[j + 1] = q.y; k[j + 2] = q.z; k[j + 3] = q.w;
+    }
+    // key before the run: the previous lane's last, or a load for lane 0
+    uint32_t prev = __shfl_up_sync(0xffffffffu, k[RI_RUN - 1], 1);
+    if (lane == 0) prev = s0 == 0 ? 0xffffffffu : (s0 <= n ? keys[b + s0 - 1] : 0xffffffffu);
+    // window of the entry before the run (-1 before the first entry)
+    int64_t rp = (s0 == 0 || prev == 0xffffffffu) ? -1 : (int64_t)min(prev >> wshift, R);
+    if (s0 < n) {
+#pragma unroll
+        for (int j = 0; j < (int)RI_RUN; j++) {
+            const uint32_t e = s0 + j;
+            const uint32_t key = k[j];
+            if (e >= n || key == 0xffffffffu) break;  // end or padding
+            const uint32_t rt = min(key >> wshift, R);
+            for (int64_t r = rp + 1; r <= (int64_t)rt; r++) ro[r] = e;
+            rp = rt;
+            // last real entry: the next key is padding or the end
+            const uint32_t nk = j + 1 < (int)RI_RUN ? k[j + 1]
+                                : (e + 1 < n ? keys[b + e + 1] : 0xffffffffu);
+            if (e + 1 == n || nk == 0xffffffffu)
+                for (uint32_t r = rt + 1; r <= R; r++) ro[r] = e + 1;
+        }
     }
     // a vector made only of padding
     if (blockIdx.x == 0 && keys[b] == 0xffffffffu)
@@ -682,33 +704,32 @@ cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, ui
 // reduction of partial blocks
 // ---------------------------------------------------------------------------
 
-// grid = ntiles, block = tile columns (one column per thread)
+// grid = (ntiles, tile rows), block = tile columns: one (row, column) pair per
+// thread, its S partials summed in segment order (double-double), so the result
+// does not depend on how the items were scheduled.
 __global__ void k_ap_reduce(ApReduceArgs r) {
     const ApTile t = r.tiles[blockIdx.x];
-    const uint32_t c = threadIdx.x;
-    if (c >= t.ncol) return;
-    const uint32_t colid = r.colids[t.col0 + c];
+    const uint32_t c = threadIdx.x, i = blockIdx.y;
+    if (c >= t.ncol || i >= t.nrow) return;
+    const uint32_t rowpos = t.row0 + i, colpos = t.col0 + c;
+    if (r.upper && !(rowpos < colpos)) return;
     const uint64_t blk = (uint64_t)r.ti * r.tj;  // float pairs per partial block
-    const FF *base = r.part + (uint64_t)blockIdx.x * r.S * blk;
-    for (uint32_t i = 0; i < t.nrow; i++) {
-        const uint32_t rowpos = t.row0 + i, colpos = t.col0 + c;
-        if (r.upper && !(rowpos < colpos)) continue;
-        DD acc = {0.0, 0.0};
-        for (uint32_t s = 0; s < r.S; s++) {
-            const FF p = base[(uint64_t)s * blk + i * r.tj + c];
-            dd_add(acc, (double)p.hi);
-            dd_add(acc, (double)p.lo);
-        }
-        const double v = __dadd_rn(acc.hi, acc.lo);
-        const uint32_t rowid = r.rowids[rowpos];
-        r.out[(uint64_t)rowid * r.ldc + colid] = v;
-        if (r.mirror) r.out[(uint64_t)colid * r.ldc + rowid] = v;
+    const FF *base = r.part + (uint64_t)blockIdx.x * r.S * blk + i * r.tj + c;
+    DD acc = {0.0, 0.0};
+    for (uint32_t s = 0; s < r.S; s++) {
+        const FF p = base[(uint64_t)s * blk];
+        dd_add(acc, (double)p.hi);
+        dd_add(acc, (double)p.lo);
     }
+    const double v = __dadd_rn(acc.hi, acc.lo);
+    const uint32_t rowid = r.rowids[rowpos], colid = r.colids[colpos];
+    r.out[(uint64_t)rowid * r.ldc + colid] = v;
+    if (r.mirror) r.out[(uint64_t)colid * r.ldc + rowid] = v;
 }
 
 cudaError_t ap_reduce_launch(const ApReduceArgs &r, cudaStream_t st) {
     if (r.ntiles == 0) return cudaSuccess;
-    k_ap_reduce<<<r.ntiles, r.tj, 0, st>>>(r);
+    k_ap_reduce<<<dim3(r.ntiles, r.ti), r.tj, 0, st>>>(r);
     return cudaGetLastError();
 }
 
