@@ -290,48 +290,37 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
         uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
         uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         uint32_t cnt0 = 0, cnt1 = 0, cnt2 = 0;
-        // this thread's windows of the tile: codes first, then the atomics of all of
-        // them, so that the returning (K-1)-mer adds are in flight together
-        constexpr int WPT = TILE / COUNT_THREADS;
-        uint32_t w2[WPT], w1[WPT], last[WPT];
-        int run[WPT];
-#pragma unroll
-        for (int u = 0; u < WPT; u++) {
+        for (int u = 0; u < TILE / COUNT_THREADS; u++) {
             const int li = u * COUNT_THREADS + threadIdx.x;
-            uint32_t w = 0;
-            w2[u] = w1[u] = last[u] = 0;
-            run[u] = 0;
-            if (start + li < len) {
+            const bool inb = start + li < len;
+            uint32_t w = 0, w2 = 0, w1 = 0, last = 0;
+            int run = 0;
+            if (inb) {
                 for (int j = 0; j < K; j++) {
                     uint32_t d = dig[li + j];
                     if (d == 0xffu) break;
                     w = w * A + d;
-                    run[u] = j + 1;
-                    if (j == K - 3) w2[u] = w;
-                    if (j == K - 2) { w1[u] = w; last[u] = d; }
+                    run = j + 1;
+                    if (j == K - 3) w2 = w;
+                    if (j == K - 2) { w1 = w; last = d; }
                 }
             }
-            cnt2 += run[u] >= K - 2; cnt1 += run[u] >= K - 1; cnt0 += run[u] >= K;
-        }
-        // counts and extension masks: reduction atomics (equal keys within a warp
-        // are rare, so no aggregation); the first sighting of a (K-1)-mer sets its
-        // seen bit (compact tables: only the seen bit here; k_c0_scatter counts
-        // once the ranks of the seen (K-1)-mers are known)
-        uint32_t old1[WPT];
-#pragma unroll
-        for (int u = 0; u < WPT; u++) {
-            if (run[u] >= K - 2) atomicAdd(&c2[w2[u]], 1u);
-            old1[u] = 1u;
-            if (run[u] >= K - 1) {
-                atomicOr(&mk[w2[u]], 1u << last[u]);
-                if (COMPACT) atomicOr(&seen[w1[u] >> 5], 1u << (w1[u] & 31u));
-                else old1[u] = atomicAdd(&c1[w1[u]], 1u);
+            const bool v2 = run >= K - 2, v1 = run >= K - 1, v0 = run >= K;
+            cnt2 += v2; cnt1 += v1; cnt0 += v0;
+            // counts and extension masks: reduction atomics (equal keys within a
+            // warp are rare, so no aggregation); the first sighting of a
+            // (K-1)-mer sets its seen bit
+            // (compact tables: only the seen bit here; k_c0_scatter counts once the
+            // ranks of the seen (K-1)-mers are known)
+            if (v2) atomicAdd(&c2[w2], 1u);
+            if (v1) {
+                if (COMPACT) {
+                    atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                } else if (atomicAdd(&c1[w1], 1u) == 0u) {
+                    atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
+                }
+                atomicOr(&mk[w2], 1u << last);
             }
-        }
-        if (!COMPACT) {
-#pragma unroll
-            for (int u = 0; u < WPT; u++)
-                if (old1[u] == 0u) atomicOr(&seen[w1[u] >> 5], 1u << (w1[u] & 31u));
         }
         // totals
         cnt0 = __reduce_add_sync(0xffffffffu, cnt0);
@@ -500,45 +489,31 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
         __syncthreads();
         const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         const uint64_t cbase = a.cbase[p];
-        // this thread's windows: codes, then the table loads of all of them, then
-        // the atomics (the loads of different windows in flight together)
-        constexpr int WPT = TILE / COUNT_THREADS;
-        uint32_t wk[WPT], bk[WPT];
-        bool v1[WPT];
-#pragma unroll
-        for (int u = 0; u < WPT; u++) {
+        for (int u = 0; u < TILE / COUNT_THREADS; u++) {
             const int li = u * COUNT_THREADS + threadIdx.x;
-            uint32_t w = 0;
-            int j = 0;
+            bool v0 = false;
+            uint64_t slot = 0;
             if (start + li < len) {
-                for (; j < K - 1; j++) {
+                uint32_t w = 0;
+                int j;
+                for (j = 0; j < K - 1; j++) {
                     uint32_t d = dig[li + j];
                     if (d == 0xffu) break;
                     w = w * A + d;
                 }
+                if (j == K - 1) {
+                    const uint64_t wi = c1_index(a, p, w);
+                    const bool in_cap = !a.compact1 || wi < a.cap1;
+                    if (a.compact1 && in_cap) atomicAdd(&a.c1[wi], 1u);  // (K-1)-window count
+                    uint32_t b = dig[li + K - 1];
+                    if (b != 0xffu && in_cap) {
+                        v0 = true;
+                        uint32_t m = a.fdT2.mod(w);
+                        slot = cbase + a.coff[wi] + __popc(mk[m] & ((1u << b) - 1u));
+                    }
+                }
             }
-            v1[u] = start + li < len && j == K - 1;  // a (K-1)-window starts here
-            wk[u] = w;
-            bk[u] = v1[u] ? dig[li + K - 1] : 0xffu;
-        }
-        uint64_t wi[WPT];
-        uint32_t co[WPT], mv[WPT];
-#pragma unroll
-        for (int u = 0; u < WPT; u++) {
-            wi[u] = v1[u] ? c1_index(a, p, wk[u]) : 0;
-            const bool kw = v1[u] && bk[u] != 0xffu && (!a.compact1 || wi[u] < a.cap1);
-            co[u] = kw ? __ldg(&a.coff[wi[u]]) : 0u;
-            mv[u] = kw ? __ldg(&mk[a.fdT2.mod(wk[u])]) : 0u;
-        }
-#pragma unroll
-        for (int u = 0; u < WPT; u++) {
-            if (!v1[u]) continue;
-            const bool in_cap = !a.compact1 || wi[u] < a.cap1;
-            if (a.compact1 && in_cap) atomicAdd(&a.c1[wi[u]], 1u);  // (K-1)-window count
-            if (bk[u] != 0xffu && in_cap) {
-                const uint64_t slot = cbase + co[u] + __popc(mv[u] & ((1u << bk[u]) - 1u));
-                if (slot < a.cand_cap) atomicAdd(&a.c0a[slot], 1u);
-            }
+            if (v0 && slot < a.cand_cap) atomicAdd(&a.c0a[slot], 1u);
         }
         __syncthreads();
     }
