@@ -526,9 +526,19 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
 // (alpha bits != 0) are compacted, in key order, to the start of their segment:
 // c0a holds their alpha bits (or TUPLE_TAG | tuple), cq their keys; seg_surv the
 // count.  Per-CTA norm partials.  grid = cand_cap / ALPHA_TILE
+//
+// Most candidates are K-mers that were not seen (count 0): their alpha is -1
+// (native.cu:392 with p = 0) and needs no table loads.  The others are listed
+// per warp in shared memory and computed densely, 32 lanes on 32 of them, so
+// the long path does not run with most lanes idle.
+constexpr int ALPHA_ILP = 2;  // listed candidates per lane in flight together
 __global__ void __launch_bounds__(CHUNK_THREADS, 3) k_alpha(BuildArgs a) {
     __shared__ U192 s_norm[CHUNK_THREADS / 32];
     __shared__ uint32_t s_m1[CHUNK_THREADS / 32], s_bad[CHUNK_THREADS / 32];
+    __shared__ uint32_t s_key[CHUNK_THREADS / 32][SEG];    // keys by segment index
+    __shared__ uint32_t s_res[CHUNK_THREADS / 32][SEG];    // stored bits by segment index
+    __shared__ uint32_t s_lcnt[CHUNK_THREADS / 32][SEG];   // listed candidates: K-mer count,
+    __shared__ uint16_t s_lidx[CHUNK_THREADS / 32][SEG];   // index in the segment
     const uint64_t c = blockIdx.x;
     const uint64_t g0 = c * ALPHA_TILE;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -556,64 +566,93 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 3) k_alpha(BuildArgs a) {
     U192 acc = {0, 0, 0};
     uint32_t m1 = 0, bad = 0, nsurv = 0;
     constexpr int NI = SEG / 32;  // candidates per lane
-    // phase 1: keys and K-mer counts of the whole segment
-    uint32_t kk[NI], full[NI];
+    // phase 1: keys and K-mer counts of the whole segment; candidates that need
+    // the long path (a seen K-mer, or a proteome without K-windows) are listed
+    uint32_t kk[NI], fl[NI];
 #pragma unroll
     for (int i = 0; i < NI; i++) {
-        const uint32_t ul = loc0 + 32 * i + lane;
+        const bool ok = loc0 + 32 * i + lane < np;
         const uint64_t u = sbase + 32 * i + lane;
-        kk[i] = ul < np ? a.cq[u] : 0u;
-        full[i] = ul < np ? a.c0a[u] : 0u;
+        kk[i] = ok ? a.cq[u] : 0u;
+        fl[i] = ok ? a.c0a[u] : 0u;
     }
-    // phase 2: alpha, four candidates per lane at a time (their table loads in flight
-    // together); an unseen K-mer (count 0) has alpha -1 and needs no count loads
+    uint32_t nlist = 0, unseen = 0;  // unseen: bit i = candidate 32 i + lane has alpha -1
 #pragma unroll
-    for (int h = 0; h < NI; h += 4) {
-        uint32_t qq[4], mm[4], bb[4], pre[4], mid[4], suf[4];
+    for (int i = 0; i < NI; i++) {
+        const bool ok = loc0 + 32 * i + lane < np;
+        s_key[w][32 * i + lane] = kk[i];
+        const bool need = ok && (fl[i] != 0u || n0 == 0u);
+        if (ok && !need) unseen |= 1u << i;
+        const unsigned bal = __ballot_sync(0xffffffffu, need);
+        if (need) {
+            const uint32_t pos = nlist + __popc(bal & ((1u << lane) - 1u));
+            s_lcnt[w][pos] = fl[i];
+            s_lidx[w][pos] = (uint16_t)(32 * i + lane);
+        }
+        nlist += __popc(bal);
+    }
+    __syncwarp();
+    // phase 2: the listed candidates, ALPHA_ILP per lane with their loads in flight together
+    for (uint32_t t0 = 0; t0 < nlist; t0 += 32 * ALPHA_ILP) {
+        uint32_t key[ALPHA_ILP], full[ALPHA_ILP], pre[ALPHA_ILP], mid[ALPHA_ILP], suf[ALPHA_ILP];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const uint32_t key = kk[h + j];
-            qq[j] = A == 21u ? key / 21u : key >> 2;  // protein or DNA alphabet
-            bb[j] = key - qq[j] * A;
-            mm[j] = a.fdT2.mod(qq[j]);
-            const bool seen = loc0 + 32 * (h + j) + lane < np && full[h + j] != 0u;
-            pre[j] = seen ? __ldg(&a.c1[c1_index(a, p, qq[j])]) : 0u;
-            mid[j] = seen ? __ldg(&c2[mm[j]]) : 0u;
-            suf[j] = seen ? __ldg(&a.c1[c1_index(a, p, mm[j] * A + bb[j])]) : 0u;
+        for (int j = 0; j < ALPHA_ILP; j++) {
+            const uint32_t t = t0 + 32 * j + lane;
+            const bool ok = t < nlist;
+            key[j] = ok ? s_key[w][s_lidx[w][t]] : 0u;
+            full[j] = ok ? s_lcnt[w][t] : 0u;
+            const uint32_t q = A == 21u ? key[j] / 21u : key[j] >> 2;  // protein or DNA alphabet
+            const uint32_t b = key[j] - q * A;
+            const uint32_t m = a.fdT2.mod(q);
+            const bool seen = ok && full[j] != 0u;
+            pre[j] = seen ? __ldg(&a.c1[c1_index(a, p, q)]) : 0u;
+            mid[j] = seen ? __ldg(&c2[m]) : 0u;
+            suf[j] = seen ? __ldg(&a.c1[c1_index(a, p, m * A + b)]) : 0u;
         }
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int i = h + j;
-            const bool ok = loc0 + 32 * i + lane < np;
-            uint32_t stored = 0;
-            float f = 0.0f;
-            if (ok) {
-                if (full[i] - 1u < 3u && pre[j] < (uint32_t)TUPLE_PS &&
-                    suf[j] < (uint32_t)TUPLE_PS && mid[j] < (uint32_t)TUPLE_MID && n0 != 0u) {
-                    const uint32_t t =
-                        ((full[i] * TUPLE_PS + pre[j]) * TUPLE_PS + suf[j]) * TUPLE_MID + mid[j];
-                    const uint32_t tb = __ldg(&atab[t]);
-                    f = __uint_as_float(tb);
-                    stored = tb ? (TUPLE_TAG | t) : 0u;
-                } else {
-                    f = markov_alpha_fast(full[i], pre[j], suf[j], mid[j], n0, n1, n2, prob);
-                    stored = __float_as_uint(f);
-                }
+        for (int j = 0; j < ALPHA_ILP; j++) {
+            const uint32_t t = t0 + 32 * j + lane;
+            if (t >= nlist) continue;
+            uint32_t stored;
+            float f;
+            if (full[j] - 1u < 3u && pre[j] < (uint32_t)TUPLE_PS && suf[j] < (uint32_t)TUPLE_PS &&
+                mid[j] < (uint32_t)TUPLE_MID && n0 != 0u) {
+                const uint32_t ti =
+                    ((full[j] * TUPLE_PS + pre[j]) * TUPLE_PS + suf[j]) * TUPLE_MID + mid[j];
+                const uint32_t tb = __ldg(&atab[ti]);
+                f = __uint_as_float(tb);
+                stored = tb ? (TUPLE_TAG | ti) : 0u;
+            } else {
+                f = markov_alpha_fast(full[j], pre[j], suf[j], mid[j], n0, n1, n2, prob);
+                stored = __float_as_uint(f);
             }
-            const bool surv = __float_as_uint(f) != 0u;
-            const unsigned bal = __ballot_sync(0xffffffffu, surv);
-            if (surv) {
-                // positions at or before this lane's own: already read (phase 1)
-                const uint64_t pos = sbase + nsurv + __popc(bal & ((1u << lane) - 1u));
-                a.c0a[pos] = stored;
-                a.cq[pos] = kk[i];
+            s_res[w][s_lidx[w][t]] = stored;
+            if (__float_as_uint(f) != 0u) {
                 const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
                 if (sq == 1.0f) m1++;
                 else if (isnan(sq)) bad |= 1u;
                 else if (isinf(sq) || !u192_add_float(acc, sq)) bad |= 2u;
             }
-            nsurv += __popc(bal);
         }
+    }
+    __syncwarp();
+    // phase 3: survivors compacted in key order to the segment's start (positions at
+    // or before a lane's own were read in phase 1); an unseen K-mer's square is 1
+    constexpr uint32_t MINUS_ONE = 0xbf800000u;  // bits of -1.0f
+#pragma unroll
+    for (int i = 0; i < NI; i++) {
+        const bool ok = loc0 + 32 * i + lane < np;
+        const bool un = (unseen >> i) & 1u;
+        const uint32_t stored = un ? MINUS_ONE : (ok ? s_res[w][32 * i + lane] : 0u);
+        const bool surv = stored != 0u;
+        const unsigned bal = __ballot_sync(0xffffffffu, surv);
+        if (surv) {
+            const uint64_t pos = sbase + nsurv + __popc(bal & ((1u << lane) - 1u));
+            a.c0a[pos] = stored;
+            a.cq[pos] = s_key[w][32 * i + lane];
+        }
+        m1 += un;
+        nsurv += __popc(bal);
     }
     if (lane == 0) a.seg_surv[seg] = nsurv;
     // norm partials (integer: exact and order independent)
