@@ -223,12 +223,24 @@ long phyloSelfDotPartBytes(int num_vectors, long max_vector_len);
  * d_union_bits: the union bitmap of the vectors' keys (bit k of uint32 word
  * k / 32, phyloKeyRankBitmapBytes bytes), as phyloBuildBatchEmit marks it; 0 to
  * build it here.  d_union_size (uint64, device) receives the union size.
- * Asynchronous. */
+ * d_rank_keys 0: only the union's prefix is built in the scratch, for
+ * phyloKeyRankIndex.  Asynchronous. */
 long phyloKeyRankScratch(long key_limit);
 long phyloKeyRankBitmapBytes(long key_limit);
 int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                   uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
                   uintptr_t d_union_bits, uintptr_t d_rank_keys, uintptr_t d_union_size);
+
+/* Ranks and window index in one pass: after phyloKeyRanks with d_rank_keys 0
+ * on the same scratch, key_limit and d_union_bits, writes the ranks of the
+ * vectors' keys to d_rank_keys and the window index over them to d_roff
+ * (uint32[num_vectors][num_windows + 1], as phyloWindowIndex on the ranks).
+ * num_windows = ceil(union size / 2^window_shift), the union size coming from
+ * phyloKeyRanks.  Arena layout as phyloWindowIndex.  Asynchronous. */
+int phyloKeyRankIndex(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
+                      uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
+                      uintptr_t d_union_bits, int window_shift, unsigned int num_windows,
+                      uintptr_t d_rank_keys, uintptr_t d_roff);
 
 /* Scratch bytes of phyloComparePairsMany for num_pairs pairs and at most
  * max_tiles merge tiles (sum over pairs of ceil((nl + nr) / 4096)). */

@@ -114,6 +114,9 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloKeyRanks.argtypes = [c_ptr, c_ptr, c_long, c_long, c_ptr, c_ptr, c_int, c_long, c_ptr,
                                 c_ptr, c_ptr]
     L.phyloKeyRanks.restype = c_int
+    L.phyloKeyRankIndex.argtypes = [c_ptr, c_ptr, c_long, c_long, c_ptr, c_ptr, c_int, c_long,
+                                    c_ptr, c_int, c_uint, c_ptr, c_ptr]
+    L.phyloKeyRankIndex.restype = c_int
     L.phyloComparePairsManyScratch.argtypes = [c_int, c_long]
     L.phyloComparePairsManyScratch.restype = c_long
     L.phyloComparePairsMany.argtypes = [c_ptr, c_ptr, c_long] + [c_ptr] * 10 + [c_int, c_long, c_ptr]
@@ -129,7 +132,7 @@ EXPORTED = [
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsThreads", "phyloPairsLaunch",
     "phyloPairsReduce",
     "phyloSelfDot", "phyloSelfDotPartBytes", "phyloKeyRankScratch", "phyloKeyRankBitmapBytes",
-    "phyloKeyRanks",
+    "phyloKeyRanks", "phyloKeyRankIndex",
     "phyloComparePairsManyScratch",
     "phyloComparePairsMany", "phyloComparePairAsync",
 ]

@@ -15,6 +15,9 @@
 //   k_rank_reduce / k_scan_partials / k_rank_prefix
 //                   exclusive prefix of the bitmap's population per 32-bit word
 //   k_rank_apply    rank = prefix[key / 32] + popc(word & bits below key)
+//   k_rank_index    the same ranks, and in the same pass the window index of the
+//                   pair kernel over them (entries of each vector below every
+//                   window start), so the ranks are not read back
 #include "rank.cuh"
 #include "scan.cuh"
 
@@ -100,6 +103,79 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_apply(const uint32_t *__res
     }
 }
 
+__device__ __forceinline__ uint32_t rank_of(uint32_t key, const uint32_t *__restrict__ bits,
+                                            const uint32_t *__restrict__ prefix) {
+    if (key == 0xffffffffu) return key;  // padding stays padding
+    const uint32_t w = key >> 5;
+    return __ldg(&prefix[w]) + (uint32_t)__popc(__ldg(&bits[w]) & ((1u << (key & 31u)) - 1u));
+}
+
+constexpr uint32_t RX_RUN = 4;                   // entries per thread
+constexpr uint32_t RX_SLICE = RK_THREADS * RX_RUN;  // entries per CTA
+
+// Ranks of RX_RUN consecutive entries per thread (16-byte loads and stores; a
+// vector starts on a 16-byte boundary and its padded length is a multiple of
+// 4), then roff[v][r] = entries of vector v with rank < r << wshift: an entry
+// whose window is above its predecessor's writes its index into the windows in
+// between; the last real entry fills the windows after it.  grid = (slices, N)
+__global__ void __launch_bounds__(RK_THREADS) k_rank_index(const uint32_t *__restrict__ keys,
+                                                           const uint64_t *__restrict__ vec_off,
+                                                           const uint32_t *__restrict__ bits,
+                                                           const uint32_t *__restrict__ prefix,
+                                                           uint32_t R, uint32_t wshift,
+                                                           uint32_t *ranks, uint32_t *roff) {
+    const uint32_t v = blockIdx.y;
+    const uint64_t b = vec_off[v];
+    const uint32_t n = (uint32_t)(vec_off[v + 1] - b);
+    uint32_t *ro = roff + (uint64_t)v * (R + 1);
+    const uint32_t e0 = blockIdx.x * RX_SLICE;
+    if (e0 >= n) {
+        if (n == 0 && blockIdx.x == 0)
+            for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const uint32_t s0 = e0 + threadIdx.x * RX_RUN;  // this thread's run
+    uint32_t k[RX_RUN];
+#pragma unroll
+    for (int j = 0; j < (int)RX_RUN; j += 4) {
+        uint4 q = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+        if (s0 + j < n) q = *reinterpret_cast<const uint4 *>(keys + b + s0 + j);
+        k[j] = q.x; k[j + 1] = q.y; k[j + 2] = q.z; k[j + 3] = q.w;
+    }
+#pragma unroll
+    for (int j = 0; j < (int)RX_RUN; j++) k[j] = rank_of(k[j], bits, prefix);
+#pragma unroll
+    for (int j = 0; j < (int)RX_RUN; j += 4)
+        if (s0 + j < n)
+            *reinterpret_cast<uint4 *>(ranks + b + s0 + j) = make_uint4(k[j], k[j + 1], k[j + 2], k[j + 3]);
+    // rank before the run: the previous lane's last, or computed for lane 0
+    uint32_t prev = __shfl_up_sync(0xffffffffu, k[RX_RUN - 1], 1);
+    if (lane == 0)
+        prev = s0 == 0 ? 0xffffffffu : (s0 <= n ? rank_of(keys[b + s0 - 1], bits, prefix) : 0xffffffffu);
+    // window of the entry before the run (-1 before the first entry)
+    int64_t rp = (s0 == 0 || prev == 0xffffffffu) ? -1 : (int64_t)min(prev >> wshift, R);
+    if (s0 < n) {
+#pragma unroll
+        for (int j = 0; j < (int)RX_RUN; j++) {
+            const uint32_t e = s0 + j;
+            const uint32_t rk = k[j];
+            if (e >= n || rk == 0xffffffffu) break;  // end or padding
+            const uint32_t rt = min(rk >> wshift, R);
+            for (int64_t r = rp + 1; r <= (int64_t)rt; r++) ro[r] = e;
+            rp = rt;
+            // last real entry: the next key is padding or the end
+            const uint32_t nk = j + 1 < (int)RX_RUN ? k[j + 1]
+                                : (e + 1 < n ? keys[b + e + 1] : 0xffffffffu);
+            if (e + 1 == n || nk == 0xffffffffu)
+                for (uint32_t r = rt + 1; r <= R; r++) ro[r] = e + 1;
+        }
+    }
+    // a vector made only of padding
+    if (blockIdx.x == 0 && keys[b] == 0xffffffffu)
+        for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
+}
+
 cudaError_t bitmap_prefix(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
                           uint32_t *prefix, uint64_t *total, cudaStream_t st) {
     const uint64_t nb = div_up(nwords ? nwords : 1, SCAN_TILE);
@@ -143,7 +219,8 @@ cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
     k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials);
     k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
     k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials, prefix, total);
-    if (N) k_rank_apply<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, bits, prefix, ranks);
+    if (N && ranks)
+        k_rank_apply<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, bits, prefix, ranks);
     if (d_union) PHYLO_CHECK(cudaMemcpyAsync(d_union, total, sizeof(uint64_t),
                                              cudaMemcpyDeviceToDevice, st));
     return cudaGetLastError();
@@ -151,5 +228,21 @@ cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
 
 // launches with a caller's bitmap: reduce, scan, prefix, apply, copy (+ mark without one)
 int key_ranks_launches(bool marked) { return marked ? 5 : 6; }
+
+cudaError_t key_rank_index(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
+                           uint64_t max_len, uint64_t key_limit, const uint32_t *union_bits,
+                           void *scratch, size_t scratch_size, uint32_t wshift, uint32_t R,
+                           uint32_t *ranks, uint32_t *roff, cudaStream_t st) {
+    const uint64_t nw = rank_words(key_limit);
+    Scratch sc(scratch, scratch_size);
+    uint32_t *own = sc.take<uint32_t>(nw);
+    uint32_t *prefix = sc.take<uint32_t>(nw);
+    if (!prefix || !ranks || !roff || wshift > 31) return cudaErrorInvalidValue;
+    if (N == 0) return cudaSuccess;
+    const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, RX_SLICE);
+    k_rank_index<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, union_bits ? union_bits : own,
+                                                         prefix, R, wshift, ranks, roff);
+    return cudaGetLastError();
+}
 
 }  // namespace phylo

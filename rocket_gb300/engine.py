@@ -372,12 +372,10 @@ class PairEngine:
         a = self.arena
         W = 1 << self.cfg.wshift
         st = _stream_handle(stream)
-        if self.cfg.compress:
-            if a.rkeys is None or a.ranked != a.n:
-                self._rank(a, st)
-            limit = a.rank_limit
-        else:
-            limit = key_limit(a.alphabet, a.k)
+        rerank = self.cfg.compress and (a.rkeys is None or a.ranked != a.n)
+        if rerank:
+            self._rank_prefix(a, st)
+        limit = a.rank_limit if self.cfg.compress else key_limit(a.alphabet, a.k)
         R = max(1, (limit + W - 1) // W)
         if (a.roff is None or a.wshift != self.cfg.wshift or a.R != R
                 or a.index_on_ranks != self.cfg.compress):
@@ -388,6 +386,16 @@ class PairEngine:
             new = torch.empty((int(a.n * 1.5) + 1, R + 1), dtype=torch.int32, device=self.device)
             new[:a.roff.shape[0]].copy_(a.roff)
             a.roff = new
+        if rerank:
+            # every vector's ranks may have changed: ranks and index in one pass
+            maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
+            check(self.L.phyloKeyRankIndex(
+                st, _p(self._rank_scratch), self._rank_scratch.numel(),
+                key_limit(a.alphabet, a.k), _p(a.keys), _p(a.vec_off), a.n, maxlen,
+                _p(a.union_bits) if self._rank_marked else 0, self.cfg.wshift, R,
+                _p(a.rkeys), _p(a.roff)))
+            self.launches += 1
+            a.ranked = a.indexed = a.n
         if a.indexed < a.n:
             maxlen = int(np.max(np.diff(a.off[a.indexed:a.n + 1])))
             check(self.L.phyloWindowIndex(
@@ -396,7 +404,9 @@ class PairEngine:
             self.launches += 1
             a.indexed = a.n
 
-    def _rank(self, a: Arena, st: int) -> None:
+    def _rank_prefix(self, a: Arena, st: int) -> None:
+        """Union bitmap prefix of the arena's keys (in the rank scratch) and the
+        union size; the ranks themselves come with the window index."""
         limit = key_limit(a.alphabet, a.k)
         nb = int(self.L.phyloKeyRankScratch(limit))
         if getattr(self, "_rank_scratch", None) is None or self._rank_scratch.numel() < nb:
@@ -405,14 +415,12 @@ class PairEngine:
             a.rkeys = torch.empty(a.keys.numel(), dtype=torch.int32, device=self.device)
         union = torch.zeros(1, dtype=torch.int64, device=self.device)
         maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
-        marked = a.union_bits is not None and a.union_n == a.n
+        self._rank_marked = a.union_bits is not None and a.union_n == a.n
         check(self.L.phyloKeyRanks(st, _p(self._rank_scratch), self._rank_scratch.numel(), limit,
                                    _p(a.keys), _p(a.vec_off), a.n, maxlen,
-                                   _p(a.union_bits) if marked else 0, _p(a.rkeys), _p(union)))
-        self.launches += 5 if marked else 6
+                                   _p(a.union_bits) if self._rank_marked else 0, 0, _p(union)))
+        self.launches += 4 if self._rank_marked else 5
         a.rank_limit = int(union.cpu().item())  # synchronises: the window count depends on it
-        a.ranked = a.n
-        a.indexed = 0  # every vector's ranks may have changed
 
     # -- planning ------------------------------------------------------------
     def _segments(self, ntiles: int) -> int:

@@ -115,7 +115,7 @@ def test_key_ranks(small):
         assert np.all(rk[o + m:end] == 0xFFFFFFFF)  # padding kept
     # the window index is built on the ranks
     roff = arena.roff.cpu().numpy()
-    for v in (0, 11):
+    for v in range(arena.n):
         r = np.searchsorted(union, keys[v])
         expect = np.searchsorted(r, np.arange(arena.R + 1, dtype=np.int64) << 10)
         assert np.array_equal(roff[v, :arena.R + 1], expect)
@@ -126,6 +126,32 @@ def test_key_ranks(small):
     eng.ensure_index()
     assert np.array_equal(arena.rkeys.cpu().numpy().view(np.uint32), rk)
     arena.union_n = saved
+
+
+@pytest.mark.parametrize("wshift", [6, 9, 11])
+def test_rank_index_matches_separate_passes(small, wshift):
+    """phyloKeyRankIndex (ranks and window index in one pass) gives the ranks of
+    phyloKeyRanks and the index phyloWindowIndex builds over them."""
+    from rocket_gb300.engine import _p, key_limit
+    p, arena, _ = small
+    eng = PairEngine(arena, EngineConfig(wshift=wshift))
+    eng.ensure_index()
+    L, n, R = eng.L, arena.n, arena.R
+    limit = key_limit(arena.alphabet, arena.k)
+    nb = int(L.phyloKeyRankScratch(limit))
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    maxlen = int(np.max(np.diff(arena.off[:n + 1])))
+    rk = torch.full_like(arena.rkeys, 7)
+    union = torch.zeros(1, dtype=torch.int64, device="cuda")
+    assert L.phyloKeyRanks(0, _p(scratch), nb, limit, _p(arena.keys), _p(arena.vec_off), n,
+                           maxlen, 0, _p(rk), _p(union)) == 0
+    roff = torch.full_like(arena.roff, 7)
+    assert L.phyloWindowIndex(0, _p(rk), _p(arena.vec_off), n, wshift, R, maxlen, _p(roff)) == 0
+    torch.cuda.synchronize()
+    assert int(union.item()) == arena.rank_limit
+    used = int(arena.off[n])
+    assert torch.equal(rk[:used], arena.rkeys[:used])
+    assert torch.equal(roff[:n, :R + 1], arena.roff[:n, :R + 1])
 
 
 def test_window_index(small):
