@@ -13,7 +13,9 @@
 //   k_rank_mark     union bitmap of the keys (reduction atomics), unless the
 //                   caller passes one (the batched build marks survivors' keys)
 //   k_rank_reduce / k_scan_partials / k_rank_prefix
-//                   exclusive prefix of the bitmap's population per 32-bit word
+//                   exclusive prefix of the bitmap's population per 32-bit word,
+//                   stored beside the word ({prefix, word} pairs: one 8-byte
+//                   gather per key, one sector, where the bitmap exceeds L2)
 //   k_rank_apply    rank = prefix[key / 32] + popc(word & bits below key)
 //   k_rank_index    the same ranks, and in the same pass the window index of the
 //                   pair kernel over them (entries of each vector below every
@@ -56,11 +58,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_rank_reduce(const uint32_t *__
     if (threadIdx.x == 0) partials[blockIdx.x] = tot;
 }
 
-// prefix[w] = keys of the union below word w; *total = union size.
+// prefix[w] = keys of the union below word w (PAIRS: pw[w] = {prefix[w], bits[w]});
+// *total = union size.
+template <bool PAIRS>
 __global__ void __launch_bounds__(SCAN_THREADS) k_rank_prefix(const uint32_t *__restrict__ bits,
                                                               uint64_t nwords,
                                                               const uint64_t *__restrict__ partials,
-                                                              uint32_t *prefix, uint64_t *total) {
+                                                              void *out, uint64_t *total) {
     __shared__ uint64_t sw[SCAN_THREADS / 32 + 1];
     const uint64_t first = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
     uint32_t c[SCAN_ITEMS];
@@ -74,17 +78,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_rank_prefix(const uint32_t *__
     uint64_t ex = block_excl_scan_u64<SCAN_THREADS>(s, sw, &tot) + partials[blockIdx.x];
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; i++) {
-        if (first + i < nwords) prefix[first + i] = (uint32_t)ex;
+        if (first + i < nwords) {
+            if (PAIRS) static_cast<uint2 *>(out)[first + i] = make_uint2((uint32_t)ex, bits[first + i]);
+            else static_cast<uint32_t *>(out)[first + i] = (uint32_t)ex;
+        }
         ex += c[i];
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total = partials[gridDim.x];
 }
 
+__device__ __forceinline__ uint32_t rank_of(uint32_t key, const uint2 *__restrict__ pw) {
+    if (key == 0xffffffffu) return key;  // padding stays padding
+    const uint2 t = __ldg(&pw[key >> 5]);
+    return t.x + (uint32_t)__popc(t.y & ((1u << (key & 31u)) - 1u));
+}
+
 // grid = (slices, N); padding keys stay 0xffffffff.
 __global__ void __launch_bounds__(RK_THREADS) k_rank_apply(const uint32_t *__restrict__ keys,
                                                            const uint64_t *__restrict__ vec_off,
-                                                           const uint32_t *__restrict__ bits,
-                                                           const uint32_t *__restrict__ prefix,
+                                                           const uint2 *__restrict__ pw,
                                                            uint32_t *ranks) {
     const uint32_t v = blockIdx.y;
     const uint64_t b = vec_off[v];
@@ -92,22 +104,7 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_apply(const uint32_t *__res
     const uint32_t e0 = blockIdx.x * RK_SLICE;
     if (e0 >= n) return;
     const uint32_t e1 = min(n, e0 + RK_SLICE);
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += RK_THREADS) {
-        const uint32_t key = keys[b + e];
-        uint32_t r = 0xffffffffu;
-        if (key != 0xffffffffu) {
-            const uint32_t w = key >> 5;
-            r = __ldg(&prefix[w]) + (uint32_t)__popc(__ldg(&bits[w]) & ((1u << (key & 31u)) - 1u));
-        }
-        ranks[b + e] = r;
-    }
-}
-
-__device__ __forceinline__ uint32_t rank_of(uint32_t key, const uint32_t *__restrict__ bits,
-                                            const uint32_t *__restrict__ prefix) {
-    if (key == 0xffffffffu) return key;  // padding stays padding
-    const uint32_t w = key >> 5;
-    return __ldg(&prefix[w]) + (uint32_t)__popc(__ldg(&bits[w]) & ((1u << (key & 31u)) - 1u));
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += RK_THREADS) ranks[b + e] = rank_of(keys[b + e], pw);
 }
 
 constexpr uint32_t RX_RUN = 4;                   // entries per thread
@@ -120,8 +117,7 @@ constexpr uint32_t RX_SLICE = RK_THREADS * RX_RUN;  // entries per CTA
 // between; the last real entry fills the windows after it.  grid = (slices, N)
 __global__ void __launch_bounds__(RK_THREADS) k_rank_index(const uint32_t *__restrict__ keys,
                                                            const uint64_t *__restrict__ vec_off,
-                                                           const uint32_t *__restrict__ bits,
-                                                           const uint32_t *__restrict__ prefix,
+                                                           const uint2 *__restrict__ pw,
                                                            uint32_t R, uint32_t wshift,
                                                            uint32_t *ranks, uint32_t *roff) {
     const uint32_t v = blockIdx.y;
@@ -144,7 +140,7 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_index(const uint32_t *__res
         k[j] = q.x; k[j + 1] = q.y; k[j + 2] = q.z; k[j + 3] = q.w;
     }
 #pragma unroll
-    for (int j = 0; j < (int)RX_RUN; j++) k[j] = rank_of(k[j], bits, prefix);
+    for (int j = 0; j < (int)RX_RUN; j++) k[j] = rank_of(k[j], pw);
 #pragma unroll
     for (int j = 0; j < (int)RX_RUN; j += 4)
         if (s0 + j < n)
@@ -152,7 +148,7 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_index(const uint32_t *__res
     // rank before the run: the previous lane's last, or computed for lane 0
     uint32_t prev = __shfl_up_sync(0xffffffffu, k[RX_RUN - 1], 1);
     if (lane == 0)
-        prev = s0 == 0 ? 0xffffffffu : (s0 <= n ? rank_of(keys[b + s0 - 1], bits, prefix) : 0xffffffffu);
+        prev = s0 == 0 ? 0xffffffffu : (s0 <= n ? rank_of(keys[b + s0 - 1], pw) : 0xffffffffu);
     // window of the entry before the run (-1 before the first entry)
     int64_t rp = (s0 == 0 || prev == 0xffffffffu) ? -1 : (int64_t)min(prev >> wshift, R);
     if (s0 < n) {
@@ -181,7 +177,7 @@ cudaError_t bitmap_prefix(const uint32_t *bits, uint64_t nwords, uint64_t *parti
     const uint64_t nb = div_up(nwords ? nwords : 1, SCAN_TILE);
     k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials);
     k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
-    k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials, prefix, total);
+    k_rank_prefix<false><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials, prefix, total);
     return cudaGetLastError();
 }
 
@@ -194,7 +190,7 @@ size_t rank_bitmap_words(uint64_t key_limit) { return rank_words(key_limit); }
 size_t rank_scratch_bytes(uint64_t key_limit) {
     const uint64_t nw = rank_words(key_limit);
     const uint64_t nb = div_up(nw, SCAN_TILE);
-    return scratch_bytes<uint32_t>(nw) + scratch_bytes<uint32_t>(nw) +
+    return scratch_bytes<uint32_t>(nw) + scratch_bytes<uint2>(nw) +
            scratch_bytes<uint64_t>(nb + 1) + scratch_bytes<uint64_t>(1);
 }
 
@@ -205,7 +201,7 @@ cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
     const uint64_t nb = div_up(nw, SCAN_TILE);
     Scratch sc(scratch, scratch_size);
     uint32_t *own = sc.take<uint32_t>(nw);
-    uint32_t *prefix = sc.take<uint32_t>(nw);
+    uint2 *pw = sc.take<uint2>(nw);
     uint64_t *partials = sc.take<uint64_t>(nb + 1);
     uint64_t *total = sc.take<uint64_t>(1);
     if (!total) return cudaErrorInvalidValue;
@@ -218,9 +214,8 @@ cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
     }
     k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials);
     k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
-    k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials, prefix, total);
-    if (N && ranks)
-        k_rank_apply<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, bits, prefix, ranks);
+    k_rank_prefix<true><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials, pw, total);
+    if (N && ranks) k_rank_apply<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, pw, ranks);
     if (d_union) PHYLO_CHECK(cudaMemcpyAsync(d_union, total, sizeof(uint64_t),
                                              cudaMemcpyDeviceToDevice, st));
     return cudaGetLastError();
@@ -235,13 +230,13 @@ cudaError_t key_rank_index(const uint32_t *keys, const uint64_t *vec_off, uint32
                            uint32_t *ranks, uint32_t *roff, cudaStream_t st) {
     const uint64_t nw = rank_words(key_limit);
     Scratch sc(scratch, scratch_size);
-    uint32_t *own = sc.take<uint32_t>(nw);
-    uint32_t *prefix = sc.take<uint32_t>(nw);
-    if (!prefix || !ranks || !roff || wshift > 31) return cudaErrorInvalidValue;
+    sc.take<uint32_t>(nw);  // the bitmap key_ranks built, unless the caller marked one
+    const uint2 *pw = sc.take<uint2>(nw);
+    (void)union_bits;       // its words are in the pairs
+    if (!pw || !ranks || !roff || wshift > 31) return cudaErrorInvalidValue;
     if (N == 0) return cudaSuccess;
     const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, RX_SLICE);
-    k_rank_index<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, union_bits ? union_bits : own,
-                                                         prefix, R, wshift, ranks, roff);
+    k_rank_index<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, pw, R, wshift, ranks, roff);
     return cudaGetLastError();
 }
 
