@@ -189,9 +189,8 @@ __device__ double u192_to_double(const U192 &a) {
 // rows of T1s entries), or its rank among the batch's seen (K-1)-mers (compact).
 __device__ __forceinline__ uint64_t c1_index(const BuildArgs &a, int p, uint32_t q) {
     if (!a.compact1) return (uint64_t)p * a.T1s + q;
-    const uint64_t w = (uint64_t)p * (a.T1s / 32) + (q >> 5);
-    return (uint64_t)__ldg(&a.prefix1[w]) +
-           (uint32_t)__popc(__ldg(&a.seen1[w]) & ((1u << (q & 31u)) - 1u));
+    const uint2 t = __ldg(&a.pw1[(uint64_t)p * (a.T1s / 32) + (q >> 5)]);  // {prefix, seen word}
+    return (uint64_t)t.x + (uint32_t)__popc(t.y & ((1u << (q & 31u)) - 1u));
 }
 
 // ---------------------------------------------------------------------------
@@ -805,7 +804,7 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     const uint64_t nw1 = g.T1s / 32 * B;
     s += scratch_bytes<uint32_t>(n1);              // c1
     s += scratch_bytes<uint32_t>(n1);              // coff
-    s += scratch_bytes<uint32_t>(compact ? nw1 : 0);                        // prefix1
+    s += scratch_bytes<uint2>(compact ? nw1 : 0);                           // pw1
     s += scratch_bytes<uint64_t>(compact ? bitmap_prefix_partials(nw1) : 0);  // p1_partials
     s += scratch_bytes<uint64_t>(1);               // p1_total
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // seen1
@@ -858,7 +857,7 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.cap1 = n1;
     r.c1 = sc.take<uint32_t>(n1);
     r.coff = sc.take<uint32_t>(n1);
-    r.prefix1 = sc.take<uint32_t>(compact ? nw1 : 0);
+    r.pw1 = sc.take<uint2>(compact ? nw1 : 0);
     r.p1_partials = sc.take<uint64_t>(compact ? bitmap_prefix_partials(nw1) : 0);
     r.p1_total = sc.take<uint64_t>(1);
     r.seen1 = sc.take<uint32_t>(g.T1s / 32 * B);
@@ -922,8 +921,8 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const int grid_seq = sm_count() * 8;
     if (a.compact1) {
         k_count<true><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
-        PHYLO_CHECK(bitmap_prefix(a.seen1, a.T1s / 32 * a.B, a.p1_partials, a.prefix1,
-                                  a.p1_total, st));
+        PHYLO_CHECK(bitmap_prefix_pairs(a.seen1, a.T1s / 32 * a.B, a.p1_partials, a.pw1,
+                                        a.p1_total, st));
     } else {
         k_count<false><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
         PHYLO_CHECK(cudaMemsetAsync(a.p1_total, 0, sizeof(uint64_t), st));

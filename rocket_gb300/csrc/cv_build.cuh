@@ -59,11 +59,11 @@ struct BuildArgs {
     uint64_t *tile_base;      // [B+1]
     // (K-1)-mer tables: dense [B][T1s] (coff written for seen (K-1)-mers only), or,
     // when `compact1` (tables beyond 2^24 entries), one entry per seen (K-1)-mer of
-    // the batch, at its rank among the seen bits: prefix1[word] + popc(bits below)
+    // the batch, at its rank among the seen bits: pw1[word].x + popc(bits below)
     uint32_t *c1, *coff;
     int compact1;
     uint64_t cap1;            // entries of c1 / coff in compact mode
-    uint32_t *prefix1;        // [B * T1s / 32]: set bits of seen1 before each word
+    uint2 *pw1;               // [B * T1s / 32]: {set bits of seen1 before the word, the word}
     uint64_t *p1_partials, *p1_total;
     uint32_t *seen1;          // [B][T1s / 32]: bitmap of the seen (K-1)-mers
     uint32_t *word_cand;      // [B][T1s / 32]: candidates of each bitmap word

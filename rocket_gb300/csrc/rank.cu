@@ -58,31 +58,26 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_rank_reduce(const uint32_t *__
     if (threadIdx.x == 0) partials[blockIdx.x] = tot;
 }
 
-// prefix[w] = keys of the union below word w (PAIRS: pw[w] = {prefix[w], bits[w]});
-// *total = union size.
-template <bool PAIRS>
+// pw[w] = {keys of the union below word w, bits[w]}; *total = union size.
 __global__ void __launch_bounds__(SCAN_THREADS) k_rank_prefix(const uint32_t *__restrict__ bits,
                                                               uint64_t nwords,
                                                               const uint64_t *__restrict__ partials,
-                                                              void *out, uint64_t *total) {
+                                                              uint2 *pw, uint64_t *total) {
     __shared__ uint64_t sw[SCAN_THREADS / 32 + 1];
     const uint64_t first = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t c[SCAN_ITEMS];
+    uint32_t wv[SCAN_ITEMS];
     uint64_t s = 0;
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; i++) {
-        c[i] = first + i < nwords ? (uint32_t)__popc(bits[first + i]) : 0u;
-        s += c[i];
+        wv[i] = first + i < nwords ? bits[first + i] : 0u;
+        s += __popc(wv[i]);
     }
     uint64_t tot;
     uint64_t ex = block_excl_scan_u64<SCAN_THREADS>(s, sw, &tot) + partials[blockIdx.x];
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; i++) {
-        if (first + i < nwords) {
-            if (PAIRS) static_cast<uint2 *>(out)[first + i] = make_uint2((uint32_t)ex, bits[first + i]);
-            else static_cast<uint32_t *>(out)[first + i] = (uint32_t)ex;
-        }
-        ex += c[i];
+        if (first + i < nwords) pw[first + i] = make_uint2((uint32_t)ex, wv[i]);
+        ex += __popc(wv[i]);
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total = partials[gridDim.x];
 }
@@ -172,12 +167,12 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_index(const uint32_t *__res
         for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
 }
 
-cudaError_t bitmap_prefix(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
-                          uint32_t *prefix, uint64_t *total, cudaStream_t st) {
+cudaError_t bitmap_prefix_pairs(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
+                                uint2 *pw, uint64_t *total, cudaStream_t st) {
     const uint64_t nb = div_up(nwords ? nwords : 1, SCAN_TILE);
     k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials);
     k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
-    k_rank_prefix<false><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials, prefix, total);
+    k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nwords, partials, pw, total);
     return cudaGetLastError();
 }
 
@@ -214,7 +209,7 @@ cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
     }
     k_rank_reduce<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials);
     k_scan_partials<<<1, SCAN_THREADS, 0, st>>>(partials, nb);
-    k_rank_prefix<true><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials, pw, total);
+    k_rank_prefix<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(bits, nw, partials, pw, total);
     if (N && ranks) k_rank_apply<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, pw, ranks);
     if (d_union) PHYLO_CHECK(cudaMemcpyAsync(d_union, total, sizeof(uint64_t),
                                              cudaMemcpyDeviceToDevice, st));

@@ -31,11 +31,12 @@ cudaError_t key_rank_index(const uint32_t *keys, const uint64_t *vec_off, uint32
                            void *scratch, size_t scratch_size, uint32_t wshift, uint32_t R,
                            uint32_t *ranks, uint32_t *roff, cudaStream_t st);
 
-// prefix[w] = set bits of words [0, w) of a bitmap (uint32 counts; the total
-// must stay below 2^32), *total = all set bits (device).  partials holds
+// pw[w] = {set bits of words [0, w) of a bitmap (uint32; the total must stay
+// below 2^32), bits[w]}: the prefix stored beside each word, so a rank lookup
+// is one 8-byte load; *total = all set bits (device).  partials holds
 // bitmap_prefix_partials(nwords) entries.  Three launches.
-cudaError_t bitmap_prefix(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
-                          uint32_t *prefix, uint64_t *total, cudaStream_t st);
+cudaError_t bitmap_prefix_pairs(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
+                                uint2 *pw, uint64_t *total, cudaStream_t st);
 uint64_t bitmap_prefix_partials(uint64_t nwords);
 
 }  // namespace phylo
