@@ -311,11 +311,13 @@ def run_ours(args):
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
     from rocket_gb300 import synth
-    from rocket_gb300.engine import BatchBuilder, EngineConfig, PairEngine
+    from rocket_gb300.engine import BatchBuilder, EngineConfig, PairEngine, auto_tile_cols
 
     wl = synth.workload(args.workload, n=args.proteomes)
     N = len(wl)
     n_pairs = N * (N - 1) // 2
+    if args.tile_cols == 0:
+        args.tile_cols = 64 if args.tile_rows == 32 else auto_tile_cols(N)
     stream = torch.cuda.current_stream(dev)
     pinned = torch.from_numpy(wl.data).pin_memory()
     seq = torch.empty(pinned.numel(), dtype=torch.uint8, device=dev)
@@ -483,6 +485,8 @@ def run_serve(args):
     rng = np.random.default_rng(4)
     sizes = rng.integers(1, 65, size=args.query_batches)
     n_db = args.db
+    if args.tile_cols == 0:  # a query batch has few row tiles: 128-column items keep the SMs busy
+        args.tile_cols = 64 if args.tile_rows == 32 else 128
     total_q = int(sizes.sum())
     t0 = time.perf_counter()
     wl = synth.workload("serve2048", n=n_db, extra=total_q + args.warmup)
@@ -560,8 +564,9 @@ def main():
                     help="pair kernel on raw keys instead of dense key ranks")
     ap.add_argument("--tile-rows", type=int, default=16, choices=[16, 32],
                     help="row vectors per pair-kernel work item (selects the kernel)")
-    ap.add_argument("--tile-cols", type=int, default=128, choices=[32, 64, 128],
-                    help="column vectors per pair-kernel work item (4 threads per column)")
+    ap.add_argument("--tile-cols", type=int, default=0, choices=[0, 32, 64, 128, 256],
+                    help="column vectors per pair-kernel work item (0: 256 for all-pair "
+                         "triangles over 384 or more proteomes, else 128)")
     ap.add_argument("--fold", type=int, default=28,
                     help="products per FP32 accumulator between compensated folds (multiple of 4)")
     ap.add_argument("--items-per-cta", type=int, default=8)

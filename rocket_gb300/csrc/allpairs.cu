@@ -111,28 +111,28 @@ __device__ __forceinline__ FF ff_shfl_xor(FF v, int m) {
     return r;
 }
 
-// Shape of a 16-row work item for a CTA of THREADS threads: four lanes per
-// column vector, so THREADS / 4 columns; each warp scatters AP_TI / warps rows,
+// Shape of a 16-row work item for a CTA of THREADS threads: LPC lanes per
+// column vector, so THREADS / LPC columns; each warp scatters AP_TI / warps rows,
 // LPR lanes per row.
-template <int THREADS>
+template <int THREADS, int LPC>
 struct ApShape {
     static constexpr int NW = THREADS / 32;
-    static constexpr int TJ = THREADS / AP_LPC;  // column vectors per item
+    static constexpr int TJ = THREADS / LPC;     // column vectors per item
     static constexpr int RPW = AP_TI / NW;       // rows a warp scatters
     static constexpr int LPR = 32 / RPW;         // lanes per scattered row
     static constexpr int NPF = RPW < AP_NPF ? AP_NPF : RPW;  // prefetched entries per lane
 };
 
-// Column side: four lanes per column vector.  Lane q of a column streams the
-// column's 4-entry groups q, q+4, q+8, ... through its cp.async ring, so the four
-// lanes of a column fetch 64 contiguous bytes per load, and keeps its own 16
-// accumulators for the whole item; the four lanes' sums are combined once, at
-// the end of the item.  Row side: lane (srow, sj) of a warp scatters entries
+// Column side: LPC lanes (4, or 2 for 256-column items) per column vector.  Lane
+// q of a column streams the column's 4-entry groups q, q+LPC, q+2 LPC, ... through
+// its cp.async ring, so the lanes of a column fetch 16 LPC contiguous bytes per
+// load, and keeps its own 16 accumulators for the whole item; the lanes' sums are
+// combined once, at the end of the item.  Row side: lane (srow, sj) of a warp scatters entries
 // sj, sj + LPR, ... of row warp * RPW + srow; the first NPF * LPR entries of each
 // row's next window are prefetched into registers.
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int LPC>
 __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
-    using S = ApShape<THREADS>;
+    using S = ApShape<THREADS, LPC>;
     constexpr int TJ = S::TJ, RPW = S::RPW, LPR = S::LPR, NPF = S::NPF;
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t W = 1u << a.wshift, wmask = W - 1u;
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
     float4 *ring_v = reinterpret_cast<float4 *>(ring_k + RING * THREADS);
     __shared__ uint32_t s_item;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t jcol = threadIdx.x / AP_LPC, q = threadIdx.x % AP_LPC;
+    const uint32_t jcol = threadIdx.x / LPC, q = threadIdx.x % LPC;
     const uint32_t srow = lane / LPR, sj = lane % LPR;
     const uint32_t rr = warp * RPW + srow;  // row position this lane scatters
     const int rsrc = (int)(srow * LPR);     // first lane of this row
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                 cp_async16(&ring_k[slot_fetch * THREADS + threadIdx.x], a.col.keys + cbase + fetch);
                 cp_async16(&ring_v[slot_fetch * THREADS + threadIdx.x], a.col.vals + cbase + fetch);
             }
-            fetch += 4 * AP_LPC;
+            fetch += 4 * LPC;
             slot_fetch = slot_fetch + 1 == RING ? 0 : slot_fetch + 1;
             cp_async_commit();
         }
@@ -285,10 +285,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                         cp_async16(&ring_v[slot_fetch * THREADS + threadIdx.x],
                                    a.col.vals + cbase + fetch);
                     }
-                    fetch += 4 * AP_LPC;
+                    fetch += 4 * LPC;
                     slot_fetch = slot_fetch + 1 == RING ? 0 : slot_fetch + 1;
                     cp_async_commit();
-                    cur += 4 * AP_LPC;
+                    cur += 4 * LPC;
                     slot_cur = slot_cur + 1 == RING ? 0 : slot_cur + 1;
                 }
             }
@@ -308,14 +308,14 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
         }
         cp_async_wait_all();
         fold16(acc, hi, lo);
-        // combine the column's four lanes (fixed order), lane q writes rows q, q+4, ...
+        // combine the column's lanes (fixed order), lane q writes rows q, q+LPC, ...
         FF *dst = a.part + (uint64_t)item.part * (AP_TI * TJ);
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             FF v = {hi[i], lo[i]};
-            v = ff_merge(v, ff_shfl_xor(v, 1));
-            v = ff_merge(v, ff_shfl_xor(v, 2));
-            if ((uint32_t)(i & 3) == q) dst[i * TJ + jcol] = v;
+#pragma unroll
+            for (int m = 1; m < LPC; m <<= 1) v = ff_merge(v, ff_shfl_xor(v, m));
+            if ((uint32_t)(i % LPC) == q) dst[i * TJ + jcol] = v;
         }
         if (a.item_cycles && threadIdx.x == 0) a.item_cycles[it] = clock64() - t_start;
     }
@@ -573,14 +573,18 @@ static size_t r32_smem_bytes(uint32_t wshift) {
 static bool r32_wide(uint32_t wshift) { return r32_smem_bytes(wshift) > 100 * 1024; }
 
 bool ap_shape_ok(int tile_rows, int tile_cols) {
-    return (tile_rows == 16 && (tile_cols == 128 || tile_cols == 64 || tile_cols == 32)) ||
+    return (tile_rows == 16 &&
+            (tile_cols == 256 || tile_cols == 128 || tile_cols == 64 || tile_cols == 32)) ||
            (tile_rows == 32 && tile_cols == 64);
 }
+
+// lanes per column vector of the 16-row kernels
+static int ap_lpc(int tile_cols) { return tile_cols == 256 ? 2 : AP_LPC; }
 
 size_t ap_smem_bytes(uint32_t wshift, int tile_rows, int tile_cols) {
     if (tile_rows == 32) return r32_smem_bytes(wshift);
     return (((size_t)1 << wshift) + 1) * D_STRIDE * sizeof(float) +
-           ap_ring_bytes(tile_cols * AP_LPC);
+           ap_ring_bytes(tile_cols * ap_lpc(tile_cols));
 }
 
 int ap_max_wshift(int tile_rows, int tile_cols) {
@@ -590,15 +594,16 @@ int ap_max_wshift(int tile_rows, int tile_cols) {
 
 int ap_threads(uint32_t wshift, int tile_rows, int tile_cols) {
     if (tile_rows == 32) return r32_wide(wshift) ? 512 : 256;
-    return tile_cols * AP_LPC;
+    return tile_cols * ap_lpc(tile_cols);
 }
 
 static const void *ap_kernel(uint32_t wshift, int tile_rows, int tile_cols) {
     if (tile_rows == 32)
         return r32_wide(wshift) ? (const void *)k_allpairs32<512, 1>
                                 : (const void *)k_allpairs32<256, 2>;
-    if (tile_cols == 128) return (const void *)k_allpairs<512, 1>;
-    return tile_cols == 32 ? (const void *)k_allpairs<128, 4> : (const void *)k_allpairs<256, 2>;
+    if (tile_cols == 256) return (const void *)k_allpairs<512, 1, 2>;
+    if (tile_cols == 128) return (const void *)k_allpairs<512, 1, 4>;
+    return tile_cols == 32 ? (const void *)k_allpairs<128, 4, 4> : (const void *)k_allpairs<256, 2, 4>;
 }
 
 cudaError_t ap_prepare(uint32_t wshift, int tile_rows, int tile_cols, int *ctas_per_sm) {
@@ -621,12 +626,14 @@ cudaError_t ap_launch(const ApArgs &a, int tile_rows, int tile_cols, int grid, c
             k_allpairs32<512, 1><<<grid, 512, smem, st>>>(a);
         else
             k_allpairs32<256, 2><<<grid, 256, smem, st>>>(a);
+    } else if (tile_cols == 256) {
+        k_allpairs<512, 1, 2><<<grid, 512, smem, st>>>(a);
     } else if (tile_cols == 128) {
-        k_allpairs<512, 1><<<grid, 512, smem, st>>>(a);
+        k_allpairs<512, 1, 4><<<grid, 512, smem, st>>>(a);
     } else if (tile_cols == 32) {
-        k_allpairs<128, 4><<<grid, 128, smem, st>>>(a);
+        k_allpairs<128, 4, 4><<<grid, 128, smem, st>>>(a);
     } else {
-        k_allpairs<256, 2><<<grid, 256, smem, st>>>(a);
+        k_allpairs<256, 2, 4><<<grid, 256, smem, st>>>(a);
     }
     return cudaGetLastError();
 }

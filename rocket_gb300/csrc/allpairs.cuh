@@ -5,7 +5,7 @@
 namespace phylo {
 
 constexpr int AP_TI = 16;             // row vectors per item (densified in shared memory)
-constexpr int AP_LPC = 4;             // lanes per column vector
+constexpr int AP_LPC = 4;             // lanes per column vector (2 for 256-column items)
 
 // One unit of work: up to tile_rows row vectors x tile_cols column vectors over
 // the key windows [w0, w1).  Vectors are named by positions in rowids / colids.
@@ -40,8 +40,9 @@ struct ApArgs {
 };
 
 // Tile shapes (tile_rows x tile_cols) select the kernel: 16 x 128 (512 threads),
-// 16 x 64 (256) and 16 x 32 (128) use 80-byte key records and four lanes per column;
-// 32 x 64 uses 128-byte swizzled records and eight lanes per column.
+// 16 x 64 (256) and 16 x 32 (128) use 80-byte key records and four lanes per column,
+// 16 x 256 (512 threads) the same records and two lanes per column; 32 x 64 uses
+// 128-byte swizzled records and eight lanes per column.
 bool ap_shape_ok(int tile_rows, int tile_cols);
 size_t ap_smem_bytes(uint32_t wshift, int tile_rows, int tile_cols);
 int ap_max_wshift(int tile_rows, int tile_cols);

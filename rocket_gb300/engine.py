@@ -47,6 +47,15 @@ def key_limit(alphabet: str, k: int) -> int:
     return NSYM[alphabet] ** k
 
 
+def auto_tile_cols(n_cols: int) -> int:
+    """Column vectors per work item for plans over ``n_cols`` columns.  Items of 256
+    columns (two lanes per column) spread each window's row scatter and barriers
+    over twice the columns, which pays once the row tiles' column spans are mostly
+    full; in a triangle over fewer than 384 vectors most 256-column items would be
+    half empty, and 128-column items keep more lanes busy."""
+    return 256 if n_cols >= 384 else 128
+
+
 # --------------------------------------------------------------------------
 # arena
 # --------------------------------------------------------------------------
@@ -351,7 +360,7 @@ class PairEngine:
         ctas = ctypes.c_int(0)
         if self.L.phyloPairsSmemBytes(self.cfg.wshift, self.cfg.tile_rows, self.cfg.tile_cols) < 0:
             raise ValueError(f"unsupported pair tile {self.cfg.tile_rows} x {self.cfg.tile_cols} "
-                             "(16 x 128, 16 x 64, 16 x 32 or 32 x 64)")
+                             "(16 x 256, 16 x 128, 16 x 64, 16 x 32 or 32 x 64)")
         check(self.L.phyloPairsPrepare(self.cfg.wshift, self.cfg.tile_rows, self.cfg.tile_cols,
                                        ctypes.byref(ctas)))
         self.ctas_per_sm = max(1, ctas.value)
@@ -438,22 +447,28 @@ class PairEngine:
         R = a.R
         row_nnz = a.nnz if row_nnz is None else row_nnz
         col_nnz = a.nnz if col_nnz is None else col_nnz
-        items = np.zeros((ntiles * S, 8), np.int64)
-        est = np.zeros(ntiles * S)
-        estp = np.zeros(ntiles * S)
-        for t, (r0, nr, c0, nc) in enumerate(tiles):
-            rn = row_nnz[rowids[r0:r0 + nr]]
-            cn = col_nnz[colids[c0:c0 + nc]]
+        tl = np.asarray(tiles, np.int64).reshape(-1, 4)
+        e_tile = np.zeros(ntiles)
+        e_prod = np.zeros(ntiles)
+        for t, (r0, nr, c0, nc) in enumerate(tl):
+            rn = row_nnz[rowids[r0:r0 + nr]].astype(np.float64)
+            cn = col_nnz[colids[c0:c0 + nc]].astype(np.float64)
             # linear model: 16 products per column entry + row scatter/clear
             # + a fixed cost per window
-            e_tile = self.cfg.tile_rows * cn.sum() + 2.0 * rn.sum() + 64.0 * R
+            e_tile[t] = self.cfg.tile_rows * cn.sum() + 2.0 * rn.sum() + 64.0 * R
             # nnz-product estimate: sum over the tile's pairs of sqrt(nnz_i * nnz_j)
-            e_prod = float(np.sqrt(np.outer(rn, cn)).sum())
-            for s in range(S):
-                i = t * S + s
-                items[i] = (r0, nr, c0, nc, s * R // S, (s + 1) * R // S, i, t)
-                est[i] = e_tile / S
-                estp[i] = e_prod / S
+            e_prod[t] = np.sqrt(rn).sum() * np.sqrt(cn).sum()
+        # item t * S + s: tile t over windows [s R / S, (s + 1) R / S)
+        t_of = np.repeat(np.arange(ntiles, dtype=np.int64), S)
+        s_of = np.tile(np.arange(S, dtype=np.int64), ntiles)
+        items = np.empty((ntiles * S, 8), np.int64)
+        items[:, 0:4] = tl[t_of]
+        items[:, 4] = s_of * R // S
+        items[:, 5] = (s_of + 1) * R // S
+        items[:, 6] = np.arange(ntiles * S, dtype=np.int64)
+        items[:, 7] = t_of
+        est = e_tile[t_of] / S
+        estp = e_prod[t_of] / S
         order = np.argsort(-est, kind="stable")
         items = items[order]
         est = est[order]
@@ -663,6 +678,7 @@ def tune_key(arena: Arena, n_rows: int, n_cols: int) -> str:
 
 
 TUNE_SPACE = [
+    dict(wshift=11, tile_rows=16, tile_cols=256, fold=28, items_per_cta=8),
     dict(wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=4),
     dict(wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=8),
     dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),

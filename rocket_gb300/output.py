@@ -57,7 +57,7 @@ def run_directory(root: str, k: int = 6, alphabet: str = "protein", device=None)
     """Reads, builds and compares every input file under `root`; returns (files, C)."""
     import torch
 
-    from .engine import BatchBuilder, PairEngine
+    from .engine import BatchBuilder, EngineConfig, PairEngine, auto_tile_cols
     from .fasta import parse_file_bytes
 
     files = scan_directory(root)
@@ -74,7 +74,7 @@ def run_directory(root: str, k: int = 6, alphabet: str = "protein", device=None)
     data = np.frombuffer(b"".join(seqs), dtype=np.uint8)
     seq = torch.from_numpy(data.copy()).to(dev)
     arena = BatchBuilder(alphabet, k, device=dev).build(seq, off)
-    engine = PairEngine(arena)
+    engine = PairEngine(arena, EngineConfig(tile_cols=auto_tile_cols(arena.n)))
     engine.ensure_index()
     out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device=dev)
     engine.run(engine.plan_triangle(), out)

@@ -62,7 +62,7 @@ def test_allpairs_matches_fp64(small, wshift, fold, rows, compress):
 
 @pytest.mark.parametrize("wshift,rows,cols", [(10, 32, 64), (9, 32, 64), (10, 16, 64),
                                               (9, 16, 32), (10, 16, 32), (11, 16, 128),
-                                              (10, 16, 128)])
+                                              (10, 16, 128), (11, 16, 256), (9, 16, 256)])
 def test_allpairs_many_tiles(many, wshift, rows, cols):
     p, arena, C_ref = many
     eng = PairEngine(arena, EngineConfig(wshift=wshift, tile_rows=rows, tile_cols=cols))
@@ -79,7 +79,7 @@ def test_tile_rows_agree(many):
     """Both kernels compute the same C to within the accumulation bound."""
     p, arena, _ = many
     outs = []
-    for rows, cols in ((16, 64), (32, 64), (16, 32)):
+    for rows, cols in ((16, 64), (32, 64), (16, 32), (16, 256)):
         eng = PairEngine(arena, EngineConfig(wshift=10, tile_rows=rows, tile_cols=cols))
         eng.ensure_index()
         out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
@@ -87,6 +87,7 @@ def test_tile_rows_agree(many):
         outs.append(out.cpu().numpy())
     assert np.abs(outs[0] - outs[1]).max() <= 3.6e-6
     assert np.abs(outs[0] - outs[2]).max() <= 3.6e-6
+    assert np.abs(outs[0] - outs[3]).max() <= 3.6e-6
 
 
 def test_rectangle_plan(small):
