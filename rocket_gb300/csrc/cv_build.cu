@@ -9,14 +9,15 @@
 //   nonzero when its prefix a.m and its suffix m.b were both seen as
 //   (K-1)-mers (then the middle m was seen too).  So the candidates are, for
 //   every seen (K-1)-mer q = a.m in ascending order, the symbols b of the
-//   right-extension set R(m) = { b : m.b seen }, kept as a 21-bit mask per
+//   right-extension set R(m) = { b : m.b seen }, a 21-bit mask per
 //   (K-2)-mer.  Enumerated in that order the candidate keys q*A + b are
 //   already sorted, and the count of every seen K-mer is scattered straight
 //   into its candidate slot (rank of b in R(m)) -- no sort and no A^K table.
 //
 // Pipeline per batch of proteomes (all kernels take the whole batch):
 //   k_prep          tile bases per proteome
-//   k_count         (K-2)/(K-1) counts, right-extension masks, window totals
+//   k_count         (K-2)/(K-1) counts, seen (K-1)-mers (the right-extension
+//                   masks are slices of that bitmap), window totals
 //   k_cand_count    candidates per chunk of 2048 (K-1)-mers
 //   scan, k_cand_bases   candidate offsets; proteome p's candidates start at
 //                   cbase[p], a multiple of ALPHA_TILE
@@ -193,6 +194,19 @@ __device__ __forceinline__ uint64_t c1_index(const BuildArgs &a, int p, uint32_t
     return (uint64_t)t.x + (uint32_t)__popc(t.y & ((1u << (q & 31u)) - 1u));
 }
 
+// Right-extension mask of (K-2)-mer m in proteome p: bit b set when the
+// (K-1)-mer m.b was seen.  Those are the A bits of the seen bitmap starting at
+// bit m * A (the code of m.b is m * A + b), so no separate table is kept.
+__device__ __forceinline__ uint32_t ext_mask(const BuildArgs &a, int p, uint32_t m) {
+    const uint32_t *sw = a.seen1 + (uint64_t)p * (a.T1s / 32);
+    const uint64_t bit = (uint64_t)m * a.A;
+    const uint64_t w = bit >> 5;
+    const uint32_t off = (uint32_t)bit & 31u;
+    uint32_t v = __ldg(&sw[w]) >> off;
+    if (off + a.A > 32u) v |= __ldg(&sw[w + 1]) << (32u - off);
+    return v & ((1u << a.A) - 1u);
+}
+
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
@@ -287,7 +301,6 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
         uint32_t *c1 = COMPACT ? nullptr : a.c1 + (uint64_t)p * a.T1s;
         uint32_t *seen = a.seen1 + (uint64_t)p * (a.T1s / 32);
         uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
-        uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         uint32_t cnt0 = 0, cnt1 = 0, cnt2 = 0;
         for (int u = 0; u < TILE / COUNT_THREADS; u++) {
             const int li = u * COUNT_THREADS + threadIdx.x;
@@ -306,11 +319,11 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             }
             const bool v2 = run >= K - 2, v1 = run >= K - 1, v0 = run >= K;
             cnt2 += v2; cnt1 += v1; cnt0 += v0;
-            // counts and extension masks: reduction atomics (equal keys within a
-            // warp are rare, so no aggregation); the first sighting of a
-            // (K-1)-mer sets its seen bit
-            // (compact tables: only the seen bit here; k_c0_scatter counts once the
-            // ranks of the seen (K-1)-mers are known)
+            // counts: reduction atomics (equal keys within a warp are rare, so no
+            // aggregation); the first sighting of a (K-1)-mer sets its seen bit,
+            // which is also bit `last` of the right-extension mask of its first
+            // K-2 symbols (compact tables: only the seen bit here; k_c0_scatter
+            // counts once the ranks of the seen (K-1)-mers are known)
             if (v2) atomicAdd(&c2[w2], 1u);
             if (v1) {
                 if (COMPACT) {
@@ -318,7 +331,6 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
                 } else if (atomicAdd(&c1[w1], 1u) == 0u) {
                     atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
                 }
-                atomicOr(&mk[w2], 1u << last);
             }
         }
         // totals
@@ -337,14 +349,14 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
 }
 
 // Candidates of the seen (K-1)-mers of one word of the seen bitmap (32
-// consecutive (K-1)-mers): |R(m)| = popc(mask[m]) for each seen q = a.m.
-__device__ __forceinline__ uint32_t word_candidates(const BuildArgs &a, const uint32_t *mk,
-                                                    uint32_t q0, uint32_t bits) {
+// consecutive (K-1)-mers): |R(m)| = popc(ext_mask(m)) for each seen q = a.m.
+__device__ __forceinline__ uint32_t word_candidates(const BuildArgs &a, int p, uint32_t q0,
+                                                    uint32_t bits) {
     uint32_t s = 0;
     while (bits) {
         const uint32_t j = __ffs(bits) - 1;
         bits &= bits - 1;
-        s += __popc(__ldg(&mk[a.fdT2.mod(q0 + j)]));
+        s += __popc(ext_mask(a, p, a.fdT2.mod(q0 + j)));
     }
     return s;
 }
@@ -356,13 +368,12 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     const int p = blockIdx.y, c = blockIdx.x;
     const uint64_t nw = a.T1s / 32;
     const uint64_t wd0 = ((uint64_t)c * CHUNK_THREADS + threadIdx.x) * a.wpt;
-    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
     uint32_t s = 0;
     for (uint32_t i = 0; i < a.wpt; i++) {
         const uint64_t wd = wd0 + i;
         if (wd >= nw) break;
         const uint32_t bits = a.seen1[(uint64_t)p * nw + wd];
-        const uint32_t sw = bits ? word_candidates(a, mk, (uint32_t)(wd * 32), bits) : 0u;
+        const uint32_t sw = bits ? word_candidates(a, p, (uint32_t)(wd * 32), bits) : 0u;
         a.word_cand[(uint64_t)p * nw + wd] = sw;
         s += sw;
     }
@@ -394,7 +405,6 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     const uint64_t pc = (uint64_t)p * a.NCH + c;
     const uint64_t nw = a.T1s / 32;
     const uint64_t wd0 = ((uint64_t)c * CHUNK_THREADS + threadIdx.x) * a.wpt;
-    const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
     uint32_t s = 0;
     for (uint32_t i = 0; i < a.wpt && wd0 + i < nw; i++) s += a.word_cand[(uint64_t)p * nw + wd0 + i];
     uint64_t tot;
@@ -421,7 +431,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
         for (int t = 0; t < 4; t++) {
             qs[t] = rest ? q0 + (uint32_t)(__ffs(rest) - 1) : 0xffffffffu;
             rest &= rest - 1;
-            ms[t] = qs[t] != 0xffffffffu ? __ldg(&mk[a.fdT2.mod(qs[t])]) : 0u;
+            ms[t] = qs[t] != 0xffffffffu ? ext_mask(a, p, a.fdT2.mod(qs[t])) : 0u;
         }
 #pragma unroll
         for (int t = 0; t < 4; t++) {
@@ -486,7 +496,6 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
             dig[j] = pos < len ? (uint8_t)char_to_digit(a.alpha, a.seq[s0 + pos]) : (uint8_t)0xff;
         }
         __syncthreads();
-        const uint32_t *mk = a.mask + (uint64_t)p * a.T2;
         const uint64_t cbase = a.cbase[p];
         for (int u = 0; u < TILE / COUNT_THREADS; u++) {
             const int li = u * COUNT_THREADS + threadIdx.x;
@@ -508,7 +517,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
                     if (b != 0xffu && in_cap) {
                         v0 = true;
                         uint32_t m = a.fdT2.mod(w);
-                        slot = cbase + a.coff[wi] + __popc(mk[m] & ((1u << b) - 1u));
+                        slot = cbase + a.coff[wi] + __popc(ext_mask(a, p, m) & ((1u << b) - 1u));
                     }
                 }
             }
@@ -810,7 +819,6 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // seen1
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // word_cand
     s += scratch_bytes<uint32_t>(g.T2 * B);        // c2
-    s += scratch_bytes<uint32_t>(g.T2 * B);        // mask
     s += scratch_bytes<uint32_t>(4 * (uint64_t)B); // tot
     s += scratch_bytes<uint64_t>(B + 1);           // seq_off (single-proteome path)
     s += scratch_bytes<uint64_t>(B + 1);           // tile_base
@@ -863,7 +871,6 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.seen1 = sc.take<uint32_t>(g.T1s / 32 * B);
     r.word_cand = sc.take<uint32_t>(g.T1s / 32 * B);
     r.c2 = sc.take<uint32_t>(g.T2 * B);
-    r.mask = sc.take<uint32_t>(g.T2 * B);
     r.tot = sc.take<uint32_t>(4 * (uint64_t)B);
     r.seq_off_store = sc.take<uint64_t>(B + 1);
     r.tile_base = sc.take<uint64_t>(B + 1);
@@ -910,11 +917,10 @@ static int sm_count() {
 // Phase 1: everything up to per-proteome nnz (no host sync inside).
 cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const uint64_t nc = (uint64_t)a.B * a.NCH;
-    // dense tables c1 | coff | c2 | mask | tot are contiguous in scratch: zero what needs it
+    // dense tables c1 | coff | c2 | tot are contiguous in scratch: zero what needs it
     if (!a.compact1) PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1s * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.seen1, 0, sizeof(uint32_t) * (a.T1s / 32) * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
-    PHYLO_CHECK(cudaMemsetAsync(a.mask, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.tot, 0, sizeof(uint32_t) * 4 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.status, 0, sizeof(uint32_t) * 4, st));
     k_prep<<<1, 32, 0, st>>>(a.B, a.seq_off, a.tile_base);

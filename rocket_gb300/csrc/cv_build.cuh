@@ -67,7 +67,7 @@ struct BuildArgs {
     uint64_t *p1_partials, *p1_total;
     uint32_t *seen1;          // [B][T1s / 32]: bitmap of the seen (K-1)-mers
     uint32_t *word_cand;      // [B][T1s / 32]: candidates of each bitmap word
-    uint32_t *c2, *mask;      // [B][T2]
+    uint32_t *c2;             // [B][T2]
     uint32_t *tot;            // [B][4]: n0, n1, n2, -
     // per (proteome, chunk of CH (K-1)-mers)
     uint32_t *chunk_cand;     // candidates per chunk
