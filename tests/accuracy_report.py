@@ -58,13 +58,15 @@ def main():
     ap.add_argument("--k", type=int, default=6)
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--tile-cols", type=int, default=128, choices=[32, 64, 128, 256],
+                    help="column vectors per pair-kernel work item (256: two lanes per column)")
     args = ap.parse_args()
 
     # CPU pool first: it must not be forked after CUDA initialises
     pool = ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 4))
     import torch
     from rocket_gb300 import synth
-    from rocket_gb300.engine import BatchBuilder, PairEngine
+    from rocket_gb300.engine import BatchBuilder, EngineConfig, PairEngine
 
     w = synth.WORKLOADS[args.workload]
     rng = np.random.default_rng(args.seed)
@@ -85,7 +87,7 @@ def main():
         if len(k) == len(oracle[i][0]):
             ulp = max(ulp, ulp_max(v, oracle[i][1]))
 
-    eng = PairEngine(arena)
+    eng = PairEngine(arena, EngineConfig(tile_cols=args.tile_cols))
     eng.ensure_index()
     C = torch.zeros((n, n), dtype=torch.float64, device="cuda")
     eng.run(eng.plan_triangle(), C)
@@ -101,7 +103,8 @@ def main():
 
     nnz = arena.nnz
     lines = [
-        f"### {args.workload}, K={args.k}: {n} proteomes sampled (seed {args.seed}), {len(pairs)} pairs",
+        f"### {args.workload}, K={args.k}: {n} proteomes sampled (seed {args.seed}), {len(pairs)} pairs, "
+        f"pair items 16 x {args.tile_cols}",
         "",
         "| check | result |",
         "|---|---|",
