@@ -19,6 +19,8 @@
 // stated.
 #include <string.h>
 
+#include <vector>
+
 #include "../../include/phylogenetics.h"
 #include "allpairs.cuh"
 #include "compare.cuh"
@@ -378,10 +380,40 @@ int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_si
     memset(&a, 0, sizeof(a));
     PHYLO_CHECK(build_carve(g, num_proteomes, (uint64_t)max_candidates, (void *)d_scratch,
                             (size_t)scratch_size, &a));
-    if (a.compact1) return (int)cudaErrorNotSupported;  // no dense (K-1)-mer rows to copy
     cudaStream_t st = (cudaStream_t)stream;
-    PHYLO_CHECK(cudaMemcpyAsync(h_c1, a.c1 + (uint64_t)p * g.T1s, sizeof(uint32_t) * g.T1,
-                                cudaMemcpyDeviceToHost, st));
+    if (a.compact1) {
+        // compact counts: entry pw1[w].x + (rank of the bit in word w) for every
+        // seen (K-1)-mer; expanded into the dense host table
+        const uint64_t nw = g.T1s / 32;
+        std::vector<uint32_t> seen(nw);
+        std::vector<uint2> pw(nw);
+        PHYLO_CHECK(cudaMemcpyAsync(seen.data(), a.seen1 + (uint64_t)p * nw, sizeof(uint32_t) * nw,
+                                    cudaMemcpyDeviceToHost, st));
+        PHYLO_CHECK(cudaMemcpyAsync(pw.data(), a.pw1 + (uint64_t)p * nw, sizeof(uint2) * nw,
+                                    cudaMemcpyDeviceToHost, st));
+        PHYLO_CHECK(cudaStreamSynchronize(st));
+        const uint64_t first = pw[0].x;
+        const uint64_t n = pw[nw - 1].x + (uint64_t)__builtin_popcount(seen[nw - 1]) - first;
+        if (first + n > a.cap1) return (int)cudaErrorInvalidValue;  // the build ran out of room
+        std::vector<uint32_t> cc(n ? n : 1);
+        if (n)
+            PHYLO_CHECK(cudaMemcpyAsync(cc.data(), a.c1 + first, sizeof(uint32_t) * n,
+                                        cudaMemcpyDeviceToHost, st));
+        PHYLO_CHECK(cudaStreamSynchronize(st));
+        memset(h_c1, 0, sizeof(uint32_t) * g.T1);
+        for (uint64_t w = 0; w < nw; w++) {
+            uint32_t bits = seen[w], r = pw[w].x - (uint32_t)first;
+            while (bits) {
+                const int j = __builtin_ctz(bits);
+                bits &= bits - 1;
+                if (w * 32 + j < g.T1) h_c1[w * 32 + j] = cc[r];
+                r++;
+            }
+        }
+    } else {
+        PHYLO_CHECK(cudaMemcpyAsync(h_c1, a.c1 + (uint64_t)p * g.T1s, sizeof(uint32_t) * g.T1,
+                                    cudaMemcpyDeviceToHost, st));
+    }
     PHYLO_CHECK(cudaMemcpyAsync(h_c2, a.c2 + (uint64_t)p * g.T2, sizeof(uint32_t) * g.T2,
                                 cudaMemcpyDeviceToHost, st));
     PHYLO_CHECK(cudaMemcpyAsync(h_tot, a.tot + (uint64_t)p * 4, sizeof(uint32_t) * 3,

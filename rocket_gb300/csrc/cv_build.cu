@@ -794,9 +794,12 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     return 0;
 }
 
-// (K-1)-mer tables beyond 2^24 entries per proteome (protein K = 7) are kept
-// compact: one entry per seen (K-1)-mer instead of a dense row.
-static bool compact1_tables(const BuildGeometry &g) { return g.T1s > (1ull << 24); }
+// (K-1)-mer tables beyond 2^20 entries per proteome (protein K >= 6) are kept
+// compact: one entry per seen (K-1)-mer instead of a dense row.  A batch's
+// dense rows (16 MB per proteome at K = 6) would live in DRAM, so every
+// (K-1)-window's count would be a DRAM atomic; the compact entries of a batch
+// stay in L2, and the zeroing of the dense rows goes away.
+static bool compact1_tables(const BuildGeometry &g) { return g.T1s > (1ull << 20); }
 
 // Candidate capacity rounded up to whole k_alpha CTAs.
 static uint64_t cand_cap_rounded(uint64_t cand_cap) {
