@@ -388,8 +388,13 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     }
 }
 
-// Keys staged per warp in shared memory before the coalesced store.
-constexpr uint32_t KEY_STAGE = 2048;
+// Keys staged per warp in shared memory before the coalesced store: 2048 for
+// dense bitmaps, 512 for sparse ones (few candidates per warp; a smaller stage
+// keeps more of these latency-bound CTAs resident).
+constexpr uint32_t KEY_STAGE = 2048, KEY_STAGE_SPARSE = 512;
+__host__ __device__ inline uint32_t key_stage(uint32_t wpt) {
+    return wpt > 1 ? KEY_STAGE_SPARSE : KEY_STAGE;
+}
 
 // coff[p][q] = candidate offset of seen (K-1)-mer q within proteome p (entries
 // of unseen q are not written); cq = the key q * A + b of every candidate (b
@@ -399,9 +404,11 @@ constexpr uint32_t KEY_STAGE = 2048;
 // stage is written directly).  grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
-    __shared__ uint32_t stage[CHUNK_THREADS / 32][KEY_STAGE];
+    extern __shared__ uint32_t stage_all[];  // [warps][key_stage(wpt)]
     const int p = blockIdx.y, c = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t kst = key_stage(a.wpt);
+    uint32_t *stage = stage_all + warp * kst;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
     const uint64_t nw = a.T1s / 32;
     const uint64_t wd0 = ((uint64_t)c * CHUNK_THREADS + threadIdx.x) * a.wpt;
@@ -415,7 +422,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     const uint32_t r0 = __shfl_sync(0xffffffffu, run, 0);
     const uint32_t r1 = __shfl_sync(0xffffffffu, run + s, 31);
     const uint64_t w0 = gb + r0, w1 = gb + r1;
-    const bool staged = r1 - r0 <= KEY_STAGE;
+    const bool staged = r1 - r0 <= kst;
     // zero this warp's K-mer count slots (coalesced)
     for (uint64_t i = w0 + lane; i < w1 && i < a.cand_cap; i += 32) a.c0a[i] = 0u;
     // this lane's candidates: seen q in ascending order, then b ascending
@@ -425,6 +432,9 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     // (every seen (K-1)-mer, also one without candidates: its compact count slot
     // is zeroed here, and it may be a candidate's suffix)
     uint32_t rest = a.seen1[(uint64_t)p * nw + wd0 + wi];
+    const uint32_t word = rest;
+    // compact tables: the rank of this word's first seen bit (one load per word)
+    const uint64_t rank0 = a.compact1 ? (uint64_t)a.pw1[(uint64_t)p * nw + wd0 + wi].x : 0;
     while (rest) {
         uint32_t qs[4], ms[4];
 #pragma unroll
@@ -437,7 +447,8 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
         for (int t = 0; t < 4; t++) {
             if (qs[t] == 0xffffffffu) break;
             const uint32_t q = qs[t];
-            const uint64_t qi = c1_index(a, p, q);
+            const uint64_t qi = a.compact1 ? rank0 + __popc(word & ((1u << (q & 31u)) - 1u))
+                                           : c1_index(a, p, q);
             if (!a.compact1 || qi < a.cap1) {
                 a.coff[qi] = run;  // no candidate: its offset is the next one's
                 if (a.compact1) a.c1[qi] = 0u;  // counted by k_c0_scatter
@@ -447,7 +458,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
                 const uint32_t key = q * A + (uint32_t)(__ffs(e) - 1);
                 e &= e - 1;
                 if (staged) {
-                    stage[warp][run - r0] = key;
+                    stage[run - r0] = key;
                 } else if (gb + run < a.cand_cap) {
                     a.cq[gb + run] = key;
                 }
@@ -459,7 +470,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     if (staged) {
         __syncwarp();
         for (uint32_t i = lane; i < r1 - r0; i += 32)
-            if (w0 + i < a.cand_cap) a.cq[w0 + i] = stage[warp][i];
+            if (w0 + i < a.cand_cap) a.cq[w0 + i] = stage[i];
     }
 }
 
@@ -789,7 +800,7 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     g->T1 = ipow64(A, k - 1);
     g->T1s = (g->T1 + 31) / 32 * 32;  // whole words of the seen bitmap
     g->T2 = ipow64(A, k - 2);
-    g->wpt = g->T1s > (1ull << 24) ? 4 : 1;  // sparse bitmaps: four words per thread
+    g->wpt = g->T1s > (1ull << 24) ? 8 : 1;  // sparse bitmaps: eight words per thread
     g->NCH = div_up(g->T1s / 32, (uint64_t)CHUNK_THREADS * g->wpt);
     return 0;
 }
@@ -942,7 +953,10 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
     k_cand_bases<<<1, 32, 0, st>>>(a);
-    k_cand_offsets<<<gch, CHUNK_THREADS, 0, st>>>(a);
+    const size_t stage_bytes = sizeof(uint32_t) * (CHUNK_THREADS / 32) * key_stage(a.wpt);
+    PHYLO_CHECK(cudaFuncSetAttribute(k_cand_offsets, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)stage_bytes));
+    k_cand_offsets<<<gch, CHUNK_THREADS, stage_bytes, st>>>(a);
     k_c0_scatter<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
     const unsigned ncta = (unsigned)(a.cand_cap / ALPHA_TILE);
     k_alpha<<<ncta, CHUNK_THREADS, 0, st>>>(a);
