@@ -236,11 +236,13 @@ int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, lon
  * vectors' keys to d_rank_keys and the window index over them to d_roff
  * (uint32[num_vectors][num_windows + 1], as phyloWindowIndex on the ranks).
  * num_windows = ceil(union size / 2^window_shift), the union size coming from
- * phyloKeyRanks.  Arena layout as phyloWindowIndex.  Asynchronous. */
+ * phyloKeyRanks.  arena_entries = vec_off[num_vectors] - vec_off[0] if known,
+ * else 0 (it only chooses the launch shape for arenas of uneven vectors).
+ * Arena layout as phyloWindowIndex.  Asynchronous. */
 int phyloKeyRankIndex(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                       uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
-                      uintptr_t d_union_bits, int window_shift, unsigned int num_windows,
-                      uintptr_t d_rank_keys, uintptr_t d_roff);
+                      long arena_entries, uintptr_t d_union_bits, int window_shift,
+                      unsigned int num_windows, uintptr_t d_rank_keys, uintptr_t d_roff);
 
 /* Scratch bytes of phyloComparePairsMany for num_pairs pairs and at most
  * max_tiles merge tiles (sum over pairs of ceil((nl + nr) / 4096)). */

@@ -115,7 +115,7 @@ def _declare(L: ctypes.CDLL) -> None:
                                 c_ptr, c_ptr]
     L.phyloKeyRanks.restype = c_int
     L.phyloKeyRankIndex.argtypes = [c_ptr, c_ptr, c_long, c_long, c_ptr, c_ptr, c_int, c_long,
-                                    c_ptr, c_int, c_uint, c_ptr, c_ptr]
+                                    c_long, c_ptr, c_int, c_uint, c_ptr, c_ptr]
     L.phyloKeyRankIndex.restype = c_int
     L.phyloComparePairsManyScratch.argtypes = [c_int, c_long]
     L.phyloComparePairsManyScratch.restype = c_long

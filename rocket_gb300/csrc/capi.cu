@@ -539,13 +539,15 @@ int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, lon
 
 int phyloKeyRankIndex(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                       uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
-                      uintptr_t d_union_bits, int window_shift, unsigned int num_windows,
-                      uintptr_t d_rank_keys, uintptr_t d_roff) {
+                      long arena_entries, uintptr_t d_union_bits, int window_shift,
+                      unsigned int num_windows, uintptr_t d_rank_keys, uintptr_t d_roff) {
     if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0 || window_shift < 0 ||
-        window_shift > 31 || scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit))
+        window_shift > 31 || arena_entries < 0 ||
+        scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit))
         return (int)cudaErrorInvalidValue;
     return (int)key_rank_index((const uint32_t *)d_keys, (const uint64_t *)d_vec_off,
-                               (uint32_t)num_vectors, (uint64_t)max_vector_len, (uint64_t)key_limit,
+                               (uint32_t)num_vectors, (uint64_t)max_vector_len,
+                               (uint64_t)arena_entries, (uint64_t)key_limit,
                                (const uint32_t *)d_union_bits, (void *)d_scratch,
                                (size_t)scratch_bytes, (uint32_t)window_shift, num_windows,
                                (uint32_t *)d_rank_keys, (uint32_t *)d_roff, (cudaStream_t)stream);

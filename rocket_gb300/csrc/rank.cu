@@ -167,6 +167,85 @@ __global__ void __launch_bounds__(RK_THREADS) k_rank_index(const uint32_t *__res
         for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
 }
 
+// k_rank_index over the whole arena as one sequence: the grid (a few CTAs per
+// SM) walks it in chunks of RX_SLICE entries, a thread's run of RX_RUN entries
+// lying in one vector (vectors are padded to multiples of 4).  For arenas of
+// very uneven vectors, where most (slice, vector) CTAs of k_rank_index would
+// have no entries.  Vectors that are empty or only padding are
+// k_rank_index_fill's.
+__global__ void __launch_bounds__(RK_THREADS) k_rank_index_flat(const uint32_t *__restrict__ keys,
+                                                           const uint64_t *__restrict__ vec_off,
+                                                           uint32_t N, const uint2 *__restrict__ pw,
+                                                           uint32_t R, uint32_t wshift,
+                                                           uint32_t *ranks, uint32_t *roff) {
+    const uint64_t a0 = vec_off[0], a1 = vec_off[N];
+    const uint64_t nchunks = div_up(a1 - a0, (uint64_t)RX_SLICE);
+    const int lane = threadIdx.x & 31;
+    uint32_t v = 0;  // this thread's vector: found once, then advanced with its runs
+    {
+        const uint64_t g = a0 + (uint64_t)blockIdx.x * RX_SLICE + threadIdx.x * RX_RUN;
+        uint32_t lo = 0, hi = N;  // last v < N with vec_off[v] <= g
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (vec_off[mid] <= g) lo = mid; else hi = mid;
+        }
+        v = lo;
+    }
+    for (uint64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const uint64_t g = a0 + ch * RX_SLICE + threadIdx.x * RX_RUN;  // this thread's run
+        const bool live = g < a1;
+        if (live)
+            while (vec_off[v + 1] <= g) v++;
+        const uint64_t b = vec_off[v];
+        const uint32_t n = (uint32_t)(vec_off[v + 1] - b);
+        const uint32_t s0 = (uint32_t)(g - b);  // position in the vector
+        uint32_t *ro = roff + (uint64_t)v * (R + 1);
+        uint32_t k[RX_RUN];
+        {
+            uint4 q = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+            if (live) q = *reinterpret_cast<const uint4 *>(keys + g);
+            k[0] = q.x; k[1] = q.y; k[2] = q.z; k[3] = q.w;
+        }
+#pragma unroll
+        for (int j = 0; j < (int)RX_RUN; j++) k[j] = rank_of(k[j], pw);
+        if (live) *reinterpret_cast<uint4 *>(ranks + g) = make_uint4(k[0], k[1], k[2], k[3]);
+        // rank before the run: the previous lane's last (the same vector unless the
+        // run starts it), or computed for lane 0
+        uint32_t prev = __shfl_up_sync(0xffffffffu, k[RX_RUN - 1], 1);
+        if (lane == 0 && live && s0 > 0) prev = rank_of(keys[g - 1], pw);
+        // window of the entry before the run (-1 before the first entry)
+        const int64_t rp0 = (s0 == 0 || prev == 0xffffffffu) ? -1 : (int64_t)min(prev >> wshift, R);
+        if (live) {
+            int64_t rp = rp0;
+#pragma unroll
+            for (int j = 0; j < (int)RX_RUN; j++) {
+                const uint32_t e = s0 + j;
+                const uint32_t rk = k[j];
+                if (rk == 0xffffffffu) break;  // padding
+                const uint32_t rt = min(rk >> wshift, R);
+                for (int64_t r = rp + 1; r <= (int64_t)rt; r++) ro[r] = e;
+                rp = rt;
+                // last real entry: the next key is padding or the end
+                const uint32_t nk = j + 1 < (int)RX_RUN ? k[j + 1]
+                                    : (e + 1 < n ? keys[b + e + 1] : 0xffffffffu);
+                if (e + 1 == n || nk == 0xffffffffu)
+                    for (uint32_t r = rt + 1; r <= R; r++) ro[r] = e + 1;
+            }
+        }
+    }
+}
+
+// roff rows of vectors that are empty or only padding: all zero.  grid = N
+__global__ void __launch_bounds__(RK_THREADS) k_rank_index_fill(const uint32_t *__restrict__ keys,
+                                                                const uint64_t *__restrict__ vec_off,
+                                                                uint32_t R, uint32_t *roff) {
+    const uint32_t v = blockIdx.x;
+    const uint64_t b = vec_off[v];
+    if (vec_off[v + 1] > b && keys[b] != 0xffffffffu) return;
+    uint32_t *ro = roff + (uint64_t)v * (R + 1);
+    for (uint32_t r = threadIdx.x; r <= R; r += blockDim.x) ro[r] = 0;
+}
+
 cudaError_t bitmap_prefix_pairs(const uint32_t *bits, uint64_t nwords, uint64_t *partials,
                                 uint2 *pw, uint64_t *total, cudaStream_t st) {
     const uint64_t nb = div_up(nwords ? nwords : 1, SCAN_TILE);
@@ -220,7 +299,8 @@ cudaError_t key_ranks(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
 int key_ranks_launches(bool marked) { return marked ? 5 : 6; }
 
 cudaError_t key_rank_index(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
-                           uint64_t max_len, uint64_t key_limit, const uint32_t *union_bits,
+                           uint64_t max_len, uint64_t entries, uint64_t key_limit,
+                           const uint32_t *union_bits,
                            void *scratch, size_t scratch_size, uint32_t wshift, uint32_t R,
                            uint32_t *ranks, uint32_t *roff, cudaStream_t st) {
     const uint64_t nw = rank_words(key_limit);
@@ -230,8 +310,19 @@ cudaError_t key_rank_index(const uint32_t *keys, const uint64_t *vec_off, uint32
     (void)union_bits;       // its words are in the pairs
     if (!pw || !ranks || !roff || wshift > 31) return cudaErrorInvalidValue;
     if (N == 0) return cudaSuccess;
-    const uint32_t slices = (uint32_t)div_up(max_len ? max_len : 1, RX_SLICE);
-    k_rank_index<<<dim3(slices, N), RK_THREADS, 0, st>>>(keys, vec_off, pw, R, wshift, ranks, roff);
+    const uint64_t slices = div_up(max_len ? max_len : 1, RX_SLICE);
+    const uint64_t chunks = div_up(entries ? entries : 1, RX_SLICE);
+    if (entries && slices * N > 2 * chunks) {  // uneven lengths: walk the arena instead
+        int dev = 0, sms = 0;
+        PHYLO_CHECK(cudaGetDevice(&dev));
+        PHYLO_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        k_rank_index_flat<<<(unsigned)(sms > 0 ? sms : 152) * 8, RK_THREADS, 0, st>>>(
+            keys, vec_off, N, pw, R, wshift, ranks, roff);
+        k_rank_index_fill<<<N, RK_THREADS, 0, st>>>(keys, vec_off, R, roff);
+    } else {
+        k_rank_index<<<dim3((unsigned)slices, N), RK_THREADS, 0, st>>>(keys, vec_off, pw, R, wshift,
+                                                                      ranks, roff);
+    }
     return cudaGetLastError();
 }
 

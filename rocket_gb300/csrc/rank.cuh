@@ -25,9 +25,13 @@ int key_ranks_launches(bool marked);
 // key limit and bitmap: the ranks of the set's keys and, in the same pass, the
 // window index over them -- roff[v][r] = entries of vector v with rank < r << wshift,
 // r = 0..R.  Vectors start on 16-byte boundaries and are padded to multiples of 4
-// entries with keys 0xffffffff.  One launch.  Asynchronous.
+// entries with keys 0xffffffff.  entries = vec_off[N] - vec_off[0] when the
+// caller knows it (0 if not): arenas of very uneven vectors are then walked as
+// one sequence (two launches) instead of by (slice, vector) CTAs (one launch).
+// Asynchronous.
 cudaError_t key_rank_index(const uint32_t *keys, const uint64_t *vec_off, uint32_t N,
-                           uint64_t max_len, uint64_t key_limit, const uint32_t *union_bits,
+                           uint64_t max_len, uint64_t entries, uint64_t key_limit,
+                           const uint32_t *union_bits,
                            void *scratch, size_t scratch_size, uint32_t wshift, uint32_t R,
                            uint32_t *ranks, uint32_t *roff, cudaStream_t st);
 

@@ -401,9 +401,11 @@ class PairEngine:
             check(self.L.phyloKeyRankIndex(
                 st, _p(self._rank_scratch), self._rank_scratch.numel(),
                 key_limit(a.alphabet, a.k), _p(a.keys), _p(a.vec_off), a.n, maxlen,
-                _p(a.union_bits) if self._rank_marked else 0, self.cfg.wshift, R,
-                _p(a.rkeys), _p(a.roff)))
-            self.launches += 1
+                int(a.off[a.n] - a.off[0]), _p(a.union_bits) if self._rank_marked else 0,
+                self.cfg.wshift, R, _p(a.rkeys), _p(a.roff)))
+            entries = int(a.off[a.n] - a.off[0])
+            flat = entries > 0 and -(-maxlen // 1024) * a.n > 2 * -(-entries // 1024)
+            self.launches += 2 if flat else 1
             a.ranked = a.indexed = a.n
         if a.indexed < a.n:
             maxlen = int(np.max(np.diff(a.off[a.indexed:a.n + 1])))

@@ -153,6 +153,20 @@ def test_rank_index_matches_separate_passes(small, wshift):
     used = int(arena.off[n])
     assert torch.equal(rk[:used], arena.rkeys[:used])
     assert torch.equal(roff[:n, :R + 1], arena.roff[:n, :R + 1])
+    # both launch shapes: (slice, vector) CTAs (arena size not given) and the walk
+    # over the whole arena (chosen for uneven vectors when the size is given)
+    entries = int(arena.off[n] - arena.off[0])
+    assert -(-maxlen // 1024) * n > 2 * -(-entries // 1024)  # this arena is uneven
+    for given in (0, entries):
+        assert L.phyloKeyRanks(0, _p(scratch), nb, limit, _p(arena.keys), _p(arena.vec_off), n,
+                               maxlen, 0, 0, _p(union)) == 0
+        rk2 = torch.full_like(arena.rkeys, 7)
+        roff2 = torch.full_like(arena.roff, 7)
+        assert L.phyloKeyRankIndex(0, _p(scratch), nb, limit, _p(arena.keys), _p(arena.vec_off), n,
+                                   maxlen, given, 0, wshift, R, _p(rk2), _p(roff2)) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(rk2[:used], rk[:used])
+        assert torch.equal(roff2[:n, :R + 1], roff[:n, :R + 1])
 
 
 def test_window_index(small):
