@@ -388,10 +388,10 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     }
 }
 
-// Keys staged per warp in shared memory before the coalesced store: 2048 for
+// Keys staged per warp in shared memory before the coalesced store: 768 for
 // dense bitmaps, 512 for sparse ones (few candidates per warp; a smaller stage
 // keeps more of these latency-bound CTAs resident).
-constexpr uint32_t KEY_STAGE = 1024, KEY_STAGE_SPARSE = 512;
+constexpr uint32_t KEY_STAGE = 768, KEY_STAGE_SPARSE = 512;
 __host__ __device__ inline uint32_t key_stage(uint32_t wpt) {
     return wpt > 1 ? KEY_STAGE_SPARSE : KEY_STAGE;
 }
