@@ -7,6 +7,8 @@ from oracle import oracle as O
 from rocket_gb300 import synth
 from rocket_gb300.engine import BatchBuilder, EngineConfig, PairEngine
 
+from gpu_helpers import ulp_diff
+
 pytestmark = pytest.mark.gpu
 
 
@@ -229,3 +231,35 @@ def test_directory_driver(tmp_path):
     assert d["files"] == [f"g{i}.faa" for i in range(5)]
     C_ref = oracle_matrix(p)
     assert np.abs(C - C_ref).max() <= 2e-6
+
+
+def test_batched_ragged_edge_proteomes():
+    """A build batch holding an empty proteome, one shorter than K, one of mostly
+    invalid symbols, one of exactly K symbols and one of short proteins, between
+    two normal ones: every vector, and every pair and self product, against the
+    oracle (NaN where the oracle has NaN)."""
+    p = synth.workload("uneven1024", n=2, scale=0.02)
+    seqs = [p.get(0), b"", b"ACD", b"XBZJOU" * 50, b"ACDEFG", b"MKV\nLLA\nWWWWWW\nAC", p.get(1)]
+    off = np.zeros(len(seqs) + 1, np.int64)
+    np.cumsum([len(s) for s in seqs], out=off[1:])
+    data = torch.from_numpy(np.frombuffer(b"".join(seqs), np.uint8).copy()).cuda()
+    arena = BatchBuilder("protein", 6, max_batch=4).build(data, off)
+    torch.cuda.synchronize()
+    ref = [O.cv_native(s, 6) for s in seqs]
+    for i, r in enumerate(ref):
+        k, v = arena.host_vector(i)
+        assert np.array_equal(k, r["keys"]), i
+        assert np.array_equal(np.isnan(v), np.isnan(r["values"])), i
+        assert ulp_diff(v, r["values"]) <= 1, i
+    eng = PairEngine(arena)
+    eng.ensure_index()
+    out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+    eng.run(eng.plan_triangle(), out)
+    C = out.cpu().numpy()
+    for i in range(len(seqs)):
+        for j in range(i, len(seqs)):
+            c = O.compare_fp64(ref[i]["keys"], ref[i]["values"], ref[j]["keys"], ref[j]["values"])
+            if np.isnan(c):
+                assert np.isnan(C[i, j]), (i, j)
+            else:
+                assert abs(C[i, j] - c) <= 2e-6, (i, j, C[i, j], c)
