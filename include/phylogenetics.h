@@ -200,8 +200,9 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
                      int tile_cols, int grid);
 
 /* Sums the partial blocks of each tile (4 uint32: row0, nrow, col0, ncol) into
- * d_out[rowid * ldc + colid] (double); `upper` keeps pairs whose row position
- * is below the column position, `mirror` also writes the transposed entry. */
+ * d_out[rowid * ldc + colid] (double); `upper` 1 keeps pairs whose row position
+ * is below the column position, 2 also the diagonal (row position == column
+ * position: the self products); `mirror` also writes the transposed entry. */
 int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
                      int segments, int tile_rows, int tile_cols, uintptr_t d_rowids,
                      uintptr_t d_colids, uintptr_t d_out, long ldc, int upper, int mirror);

@@ -719,7 +719,8 @@ __global__ void k_ap_reduce(ApReduceArgs r) {
     const uint32_t c = threadIdx.x, i = blockIdx.y;
     if (c >= t.ncol || i >= t.nrow) return;
     const uint32_t rowpos = t.row0 + i, colpos = t.col0 + c;
-    if (r.upper && !(rowpos < colpos)) return;
+    if (r.upper == 1 && !(rowpos < colpos)) return;
+    if (r.upper == 2 && !(rowpos <= colpos)) return;  // with the diagonal
     const uint64_t blk = (uint64_t)r.ti * r.tj;  // float pairs per partial block
     const FF *base = r.part + (uint64_t)blockIdx.x * r.S * blk + i * r.tj + c;
     DD acc = {0.0, 0.0};

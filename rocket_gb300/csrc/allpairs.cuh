@@ -57,7 +57,8 @@ cudaError_t range_index_launch(const uint32_t *keys, const uint64_t *vec_off, ui
 
 // Tile t (rows rowids[row0..], columns colids[col0..]) has S partial blocks
 // part[t * S + s].  Writes out[rowid * ldc + colid] (and the mirrored entry
-// when `mirror`), for pairs with row position < column position when `upper`.
+// when `mirror`), for pairs with row position < column position when `upper` is
+// 1, <= when it is 2.
 struct ApTile {
     uint32_t row0, nrow, col0, ncol;
 };

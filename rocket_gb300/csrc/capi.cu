@@ -498,7 +498,7 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
 int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
                      int segments, int tile_rows, int tile_cols, uintptr_t d_rowids,
                      uintptr_t d_colids, uintptr_t d_out, long ldc, int upper, int mirror) {
-    if (!ap_shape_ok(tile_rows, tile_cols)) return (int)cudaErrorInvalidValue;
+    if (!ap_shape_ok(tile_rows, tile_cols) || upper < 0 || upper > 2) return (int)cudaErrorInvalidValue;
     ApReduceArgs r;
     r.part = (const FF *)d_part;
     r.tiles = (const ApTile *)d_tiles;

@@ -335,6 +335,7 @@ class PairPlan:
     est_product: np.ndarray    # nnz-product estimate per item
     pairs: int                 # valid pairs covered
     host_items: np.ndarray = field(default=None)
+    diag: bool = False         # the tiles also cover every vector with itself
 
 
 @dataclass
@@ -493,14 +494,18 @@ class PairEngine:
         N = len(perm)
         tiles = []
         ti, tj = self.cfg.tile_rows, self.cfg.tile_cols
+        # columns from the tile's first row: every vector meets itself too (the self
+        # products, the diagonal of the reference's matrix, Main.java:196)
         for r0 in range(0, N, ti):
             nr = min(ti, N - r0)
-            c = r0 + 1
+            c = r0
             while c < N:
                 nc = min(tj, N - c)
                 tiles.append((r0, nr, c, nc))
                 c += nc
-        return self._finish_plan(perm, perm, tiles, True, True, ldc or a.n, N * (N - 1) // 2)
+        plan = self._finish_plan(perm, perm, tiles, True, True, ldc or a.n, N * (N - 1) // 2)
+        plan.diag = True
+        return plan
 
     def plan_rect(self, row_ids: Sequence[int], col_ids: Sequence[int], ldc: int,
                   col_arena: Optional[Arena] = None) -> PairPlan:
@@ -554,10 +559,10 @@ class PairEngine:
             events[1].record(s_obj)
         check(self.L.phyloPairsReduce(
             st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, self.cfg.tile_rows, self.cfg.tile_cols,
-            _p(plan.rowids), _p(plan.colids), _p(out), plan.ldc, int(plan.upper),
-            int(plan.mirror)))
+            _p(plan.rowids), _p(plan.colids), _p(out), plan.ldc,
+            (2 if plan.diag and diagonal else 1) if plan.upper else 0, int(plan.mirror)))
         self.launches += 3  # counter fill, pair kernel, reduction
-        if diagonal and plan.upper:
+        if diagonal and plan.upper and not plan.diag:
             maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
             nb = int(self.L.phyloSelfDotPartBytes(a.n, maxlen))
             if self.self_part is None or self.self_part.numel() < nb:
@@ -565,10 +570,10 @@ class PairEngine:
             check(self.L.phyloSelfDot(st, _p(a.values), _p(a.vec_off), a.n, maxlen,
                                       _p(self.self_part), _p(out), plan.ldc))
             self.launches += 2
-        self._fix_nonfinite(plan, out, s_obj, col_arena)
+        self._fix_nonfinite(plan, out, s_obj, col_arena, diag=diagonal and plan.diag)
 
     def _fix_nonfinite(self, plan: PairPlan, out: torch.Tensor, stream,
-                       col_arena: Optional[Arena] = None) -> None:
+                       col_arena: Optional[Arena] = None, diag: bool = False) -> None:
         """Vectors whose values are NaN/inf: recompute their pairs with the
         merge-path kernel, which only multiplies values of shared keys (as the
         reference does)."""
@@ -591,7 +596,7 @@ class PairEngine:
             for i in range(r0, r0 + nr):
                 for j in range(c0, c0 + nc):
                     r, c = int(rows[i]), int(cols[j])
-                    if plan.upper and not i < j:
+                    if plan.upper and not (i < j or (diag and i == j)):
                         continue
                     if r not in bad_r and c not in bad_c:
                         continue
