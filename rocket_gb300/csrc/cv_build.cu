@@ -428,44 +428,44 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     // this lane's candidates: seen q in ascending order, then b ascending
     const uint32_t A = a.A;
     for (uint32_t wi = 0; wi < a.wpt && wd0 + wi < nw; wi++) {
-    const uint32_t q0 = (uint32_t)((wd0 + wi) * 32);
-    // (every seen (K-1)-mer, also one without candidates: its compact count slot
-    // is zeroed here, and it may be a candidate's suffix)
-    uint32_t rest = a.seen1[(uint64_t)p * nw + wd0 + wi];
-    const uint32_t word = rest;
-    // compact tables: the rank of this word's first seen bit (one load per word)
-    const uint64_t rank0 = a.compact1 ? (uint64_t)a.pw1[(uint64_t)p * nw + wd0 + wi].x : 0;
-    while (rest) {
-        uint32_t qs[4], ms[4];
+        const uint32_t q0 = (uint32_t)((wd0 + wi) * 32);
+        // (every seen (K-1)-mer, also one without candidates: its compact count slot
+        // is zeroed here, and it may be a candidate's suffix)
+        uint32_t rest = a.seen1[(uint64_t)p * nw + wd0 + wi];
+        const uint32_t word = rest;
+        // compact tables: the rank of this word's first seen bit (one load per word)
+        const uint64_t rank0 = a.compact1 ? (uint64_t)a.pw1[(uint64_t)p * nw + wd0 + wi].x : 0;
+        while (rest) {
+            uint32_t qs[4], ms[4];
 #pragma unroll
-        for (int t = 0; t < 4; t++) {
-            qs[t] = rest ? q0 + (uint32_t)(__ffs(rest) - 1) : 0xffffffffu;
-            rest &= rest - 1;
-            ms[t] = qs[t] != 0xffffffffu ? ext_mask(a, p, a.fdT2.mod(qs[t])) : 0u;
-        }
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-            if (qs[t] == 0xffffffffu) break;
-            const uint32_t q = qs[t];
-            const uint64_t qi = a.compact1 ? rank0 + __popc(word & ((1u << (q & 31u)) - 1u))
-                                           : c1_index(a, p, q);
-            if (!a.compact1 || qi < a.cap1) {
-                a.coff[qi] = run;  // no candidate: its offset is the next one's
-                if (a.compact1) a.c1[qi] = 0u;  // counted by k_c0_scatter
+            for (int t = 0; t < 4; t++) {
+                qs[t] = rest ? q0 + (uint32_t)(__ffs(rest) - 1) : 0xffffffffu;
+                rest &= rest - 1;
+                ms[t] = qs[t] != 0xffffffffu ? ext_mask(a, p, a.fdT2.mod(qs[t])) : 0u;
             }
-            uint32_t e = ms[t];
-            while (e) {
-                const uint32_t key = q * A + (uint32_t)(__ffs(e) - 1);
-                e &= e - 1;
-                if (staged) {
-                    stage[run - r0] = key;
-                } else if (gb + run < a.cand_cap) {
-                    a.cq[gb + run] = key;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                if (qs[t] == 0xffffffffu) break;
+                const uint32_t q = qs[t];
+                const uint64_t qi = a.compact1 ? rank0 + __popc(word & ((1u << (q & 31u)) - 1u))
+                                               : c1_index(a, p, q);
+                if (!a.compact1 || qi < a.cap1) {
+                    a.coff[qi] = run;  // no candidate: its offset is the next one's
+                    if (a.compact1) a.c1[qi] = 0u;  // counted by k_c0_scatter
                 }
-                run++;
+                uint32_t e = ms[t];
+                while (e) {
+                    const uint32_t key = q * A + (uint32_t)(__ffs(e) - 1);
+                    e &= e - 1;
+                    if (staged) {
+                        stage[run - r0] = key;
+                    } else if (gb + run < a.cand_cap) {
+                        a.cq[gb + run] = key;
+                    }
+                    run++;
+                }
             }
         }
-    }
     }
     if (staged) {
         __syncwarp();
