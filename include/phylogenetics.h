@@ -142,8 +142,9 @@ int phyloBuildBatchNorms(uintptr_t stream, uintptr_t d_scratch, long scratch_siz
 
 /* Dense (K-1)- and (K-2)-mer count tables and n0/n1/n2 of proteome p of the
  * last Plan (host buffers of A^(K-1), A^(K-2) and 3 uint32).  Where the build
- * keeps the (K-1)-mer counts compact (one entry per seen (K-1)-mer, tables
- * beyond 2^20 entries: protein K >= 6), they are expanded here on the host. */
+ * keeps counts compact (one entry per seen (K-1)- or (K-2)-mer, tables beyond
+ * 2^20 entries: the (K-1)-mer counts from protein K = 6, the (K-2)-mer counts at
+ * protein K = 7), they are expanded here on the host. */
 int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
                           const char *alphabet, int k, int num_proteomes, long max_candidates,
                           int p, uint32_t *h_c1, uint32_t *h_c2, uint32_t *h_tot);

@@ -369,6 +369,40 @@ int phyloBuildBatchNorms(uintptr_t stream, uintptr_t d_scratch, long scratch_siz
 
 // Dense (K-1)- and (K-2)-mer count tables and n0/n1/n2 of proteome p of the last
 // Plan (for count-parity checks).  Synchronous.
+// Compact count table of proteome p (entry pw[w].x + rank of the bit in word w for
+// every set bit of the seen bitmap's nw words) expanded into a dense host table of
+// `len` entries.
+static cudaError_t expand_compact_counts(const uint32_t *d_seen, const uint2 *d_pw,
+                                         const uint32_t *d_counts, uint64_t cap, uint64_t nw,
+                                         int p, uint64_t len, uint32_t *h_out, cudaStream_t st) {
+    std::vector<uint32_t> seen(nw);
+    std::vector<uint2> pw(nw);
+    PHYLO_CHECK(cudaMemcpyAsync(seen.data(), d_seen + (uint64_t)p * nw, sizeof(uint32_t) * nw,
+                                cudaMemcpyDeviceToHost, st));
+    PHYLO_CHECK(cudaMemcpyAsync(pw.data(), d_pw + (uint64_t)p * nw, sizeof(uint2) * nw,
+                                cudaMemcpyDeviceToHost, st));
+    PHYLO_CHECK(cudaStreamSynchronize(st));
+    const uint64_t first = pw[0].x;
+    const uint64_t n = pw[nw - 1].x + (uint64_t)__builtin_popcount(seen[nw - 1]) - first;
+    if (first + n > cap) return cudaErrorInvalidValue;  // the build ran out of room
+    std::vector<uint32_t> cc(n ? n : 1);
+    if (n)
+        PHYLO_CHECK(cudaMemcpyAsync(cc.data(), d_counts + first, sizeof(uint32_t) * n,
+                                    cudaMemcpyDeviceToHost, st));
+    PHYLO_CHECK(cudaStreamSynchronize(st));
+    memset(h_out, 0, sizeof(uint32_t) * len);
+    for (uint64_t w = 0; w < nw; w++) {
+        uint32_t bits = seen[w], r = pw[w].x - (uint32_t)first;
+        while (bits) {
+            const int j = __builtin_ctz(bits);
+            bits &= bits - 1;
+            if (w * 32 + j < len) h_out[w * 32 + j] = cc[r];
+            r++;
+        }
+    }
+    return cudaSuccess;
+}
+
 int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
                           const char *alphabet, int k, int num_proteomes, long max_candidates,
                           int p, uint32_t *h_c1, uint32_t *h_c2, uint32_t *h_tot) {
@@ -382,40 +416,17 @@ int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_si
                             (size_t)scratch_size, &a));
     cudaStream_t st = (cudaStream_t)stream;
     if (a.compact1) {
-        // compact counts: entry pw1[w].x + (rank of the bit in word w) for every
-        // seen (K-1)-mer; expanded into the dense host table
-        const uint64_t nw = g.T1s / 32;
-        std::vector<uint32_t> seen(nw);
-        std::vector<uint2> pw(nw);
-        PHYLO_CHECK(cudaMemcpyAsync(seen.data(), a.seen1 + (uint64_t)p * nw, sizeof(uint32_t) * nw,
-                                    cudaMemcpyDeviceToHost, st));
-        PHYLO_CHECK(cudaMemcpyAsync(pw.data(), a.pw1 + (uint64_t)p * nw, sizeof(uint2) * nw,
-                                    cudaMemcpyDeviceToHost, st));
-        PHYLO_CHECK(cudaStreamSynchronize(st));
-        const uint64_t first = pw[0].x;
-        const uint64_t n = pw[nw - 1].x + (uint64_t)__builtin_popcount(seen[nw - 1]) - first;
-        if (first + n > a.cap1) return (int)cudaErrorInvalidValue;  // the build ran out of room
-        std::vector<uint32_t> cc(n ? n : 1);
-        if (n)
-            PHYLO_CHECK(cudaMemcpyAsync(cc.data(), a.c1 + first, sizeof(uint32_t) * n,
-                                        cudaMemcpyDeviceToHost, st));
-        PHYLO_CHECK(cudaStreamSynchronize(st));
-        memset(h_c1, 0, sizeof(uint32_t) * g.T1);
-        for (uint64_t w = 0; w < nw; w++) {
-            uint32_t bits = seen[w], r = pw[w].x - (uint32_t)first;
-            while (bits) {
-                const int j = __builtin_ctz(bits);
-                bits &= bits - 1;
-                if (w * 32 + j < g.T1) h_c1[w * 32 + j] = cc[r];
-                r++;
-            }
-        }
+        PHYLO_CHECK(expand_compact_counts(a.seen1, a.pw1, a.c1, a.cap1, g.T1s / 32, p, g.T1, h_c1, st));
     } else {
         PHYLO_CHECK(cudaMemcpyAsync(h_c1, a.c1 + (uint64_t)p * g.T1s, sizeof(uint32_t) * g.T1,
                                     cudaMemcpyDeviceToHost, st));
     }
-    PHYLO_CHECK(cudaMemcpyAsync(h_c2, a.c2 + (uint64_t)p * g.T2, sizeof(uint32_t) * g.T2,
-                                cudaMemcpyDeviceToHost, st));
+    if (a.compact2) {
+        PHYLO_CHECK(expand_compact_counts(a.seen2, a.pw2, a.c2, a.cap2, g.T2s / 32, p, g.T2, h_c2, st));
+    } else {
+        PHYLO_CHECK(cudaMemcpyAsync(h_c2, a.c2 + (uint64_t)p * g.T2, sizeof(uint32_t) * g.T2,
+                                    cudaMemcpyDeviceToHost, st));
+    }
     PHYLO_CHECK(cudaMemcpyAsync(h_tot, a.tot + (uint64_t)p * 4, sizeof(uint32_t) * 3,
                                 cudaMemcpyDeviceToHost, st));
     PHYLO_CHECK(cudaStreamSynchronize(st));

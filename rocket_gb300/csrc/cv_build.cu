@@ -194,6 +194,14 @@ __device__ __forceinline__ uint64_t c1_index(const BuildArgs &a, int p, uint32_t
     return (uint64_t)t.x + (uint32_t)__popc(t.y & ((1u << (q & 31u)) - 1u));
 }
 
+// Index of (K-2)-mer m of proteome p in c2: dense row entry, or its rank among
+// the batch's seen (K-2)-mers (compact).
+__device__ __forceinline__ uint64_t c2_index(const BuildArgs &a, int p, uint32_t m) {
+    if (!a.compact2) return (uint64_t)p * a.T2 + m;
+    const uint2 t = __ldg(&a.pw2[(uint64_t)p * (a.T2s / 32) + (m >> 5)]);
+    return (uint64_t)t.x + (uint32_t)__popc(t.y & ((1u << (m & 31u)) - 1u));
+}
+
 // Right-extension mask of (K-2)-mer m in proteome p: bit b set when the
 // (K-1)-mer m.b was seen.  Those are the A bits of the seen bitmap starting at
 // bit m * A (the code of m.b is m * A + b), so no separate table is kept.
@@ -301,6 +309,7 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
         uint32_t *c1 = COMPACT ? nullptr : a.c1 + (uint64_t)p * a.T1s;
         uint32_t *seen = a.seen1 + (uint64_t)p * (a.T1s / 32);
         uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
+        uint32_t *seen2 = a.seen2 + (uint64_t)p * (a.T2s / 32);
         uint32_t cnt0 = 0, cnt1 = 0, cnt2 = 0;
         for (int u = 0; u < TILE / COUNT_THREADS; u++) {
             const int li = u * COUNT_THREADS + threadIdx.x;
@@ -324,7 +333,10 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count(BuildArgs a) {
             // which is also bit `last` of the right-extension mask of its first
             // K-2 symbols (compact tables: only the seen bit here; k_c0_scatter
             // counts once the ranks of the seen (K-1)-mers are known)
-            if (v2) atomicAdd(&c2[w2], 1u);
+            if (v2) {  // compact (K-2)-mer tables: the seen bit; k_c0_scatter counts
+                if (a.compact2) atomicOr(&seen2[w2 >> 5], 1u << (w2 & 31u));
+                else atomicAdd(&c2[w2], 1u);
+            }
             if (v1) {
                 if (COMPACT) {
                     atomicOr(&seen[w1 >> 5], 1u << (w1 & 31u));
@@ -489,6 +501,7 @@ __global__ void k_cand_bases(BuildArgs a) {
     *a.cand_total = run;
     if (run > a.cand_cap) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
     if (a.compact1 && *a.p1_total > a.cap1) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
+    if (a.compact2 && *a.p2_total > a.cap2) atomicOr(a.status, (uint32_t)DEV_CAPACITY);
 }
 
 // Every K-window adds one to the slot of its candidate (native.cu:244); with
@@ -513,12 +526,17 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
             bool v0 = false;
             uint64_t slot = 0;
             if (start + li < len) {
-                uint32_t w = 0;
+                uint32_t w = 0, w2 = 0;
                 int j;
                 for (j = 0; j < K - 1; j++) {
+                    if (j == K - 2) w2 = w;  // the first K-2 symbols
                     uint32_t d = dig[li + j];
                     if (d == 0xffu) break;
                     w = w * A + d;
+                }
+                if (a.compact2 && j >= K - 2) {  // a (K-2)-window starts here: its count
+                    const uint64_t mi = c2_index(a, p, w2);
+                    if (mi < a.cap2) atomicAdd(&a.c2[mi], 1u);
                 }
                 if (j == K - 1) {
                     const uint64_t wi = c1_index(a, p, w);
@@ -575,7 +593,6 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 5) k_alpha(BuildArgs a) {
     const int p = find_owner(a.cbase, a.B, g0);
     const uint32_t np =
         (uint32_t)(a.chunk_cand_off[(uint64_t)(p + 1) * a.NCH] - a.chunk_cand_off[(uint64_t)p * a.NCH]);
-    const uint32_t *c2 = a.c2 + (uint64_t)p * a.T2;
     const double *prob = a.prob + (uint64_t)p * 4 * PROB_TABLE;
     const uint32_t *atab = a.atab + (uint64_t)p * TUPLE_TABLE;
     const uint32_t n0 = a.tot[p * 4 + 0], n1 = a.tot[p * 4 + 1], n2 = a.tot[p * 4 + 2];
@@ -625,7 +642,8 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 5) k_alpha(BuildArgs a) {
             const uint32_t m = a.fdT2.mod(q);
             const bool seen = ok && full[j] != 0u;
             pre[j] = seen ? __ldg(&a.c1[c1_index(a, p, q)]) : 0u;
-            mid[j] = seen ? __ldg(&c2[m]) : 0u;
+            const uint64_t mi = seen ? c2_index(a, p, m) : 0;
+            mid[j] = seen && (!a.compact2 || mi < a.cap2) ? __ldg(&a.c2[mi]) : 0u;
             suf[j] = seen ? __ldg(&a.c1[c1_index(a, p, m * A + b)]) : 0u;
         }
 #pragma unroll
@@ -800,6 +818,7 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     g->T1 = ipow64(A, k - 1);
     g->T1s = (g->T1 + 31) / 32 * 32;  // whole words of the seen bitmap
     g->T2 = ipow64(A, k - 2);
+    g->T2s = (g->T2 + 31) / 32 * 32;
     g->wpt = g->T1s > (1ull << 24) ? 8 : 1;  // sparse bitmaps: eight words per thread
     g->NCH = div_up(g->T1s / 32, (uint64_t)CHUNK_THREADS * g->wpt);
     return 0;
@@ -811,6 +830,8 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
 // (K-1)-window's count would be a DRAM atomic; the compact entries of a batch
 // stay in L2, and the zeroing of the dense rows goes away.
 static bool compact1_tables(const BuildGeometry &g) { return g.T1s > (1ull << 20); }
+// (K-2)-mer counts likewise beyond 2^20 entries (protein K = 7: 16 MB per proteome).
+static bool compact2_tables(const BuildGeometry &g) { return g.T2s > (1ull << 20); }
 
 // Candidate capacity rounded up to whole k_alpha CTAs.
 static uint64_t cand_cap_rounded(uint64_t cand_cap) {
@@ -832,7 +853,13 @@ size_t build_scratch_bytes(const BuildGeometry &g, int B, uint64_t cand_cap) {
     s += scratch_bytes<uint64_t>(1);               // p1_total
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // seen1
     s += scratch_bytes<uint32_t>(g.T1s / 32 * B);  // word_cand
-    s += scratch_bytes<uint32_t>(g.T2 * B);        // c2
+    const bool compact2 = compact2_tables(g);
+    const uint64_t nw2 = g.T2s / 32 * B;
+    s += scratch_bytes<uint32_t>(compact2 ? cap : g.T2 * B);                    // c2
+    s += scratch_bytes<uint32_t>(compact2 ? nw2 : 0);                           // seen2
+    s += scratch_bytes<uint2>(compact2 ? nw2 : 0);                              // pw2
+    s += scratch_bytes<uint64_t>(compact2 ? bitmap_prefix_partials(nw2) : 0);  // p2_partials
+    s += scratch_bytes<uint64_t>(1);                                            // p2_total
     s += scratch_bytes<uint32_t>(4 * (uint64_t)B); // tot
     s += scratch_bytes<uint64_t>(B + 1);           // seq_off (single-proteome path)
     s += scratch_bytes<uint64_t>(B + 1);           // tile_base
@@ -884,7 +911,16 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     r.p1_total = sc.take<uint64_t>(1);
     r.seen1 = sc.take<uint32_t>(g.T1s / 32 * B);
     r.word_cand = sc.take<uint32_t>(g.T1s / 32 * B);
-    r.c2 = sc.take<uint32_t>(g.T2 * B);
+    const bool compact2 = compact2_tables(g);
+    const uint64_t nw2 = g.T2s / 32 * B;
+    r.compact2 = compact2 ? 1 : 0;
+    r.cap2 = compact2 ? cap : g.T2 * B;
+    r.T2s = g.T2s;
+    r.c2 = sc.take<uint32_t>(r.cap2);
+    r.seen2 = sc.take<uint32_t>(compact2 ? nw2 : 0);
+    r.pw2 = sc.take<uint2>(compact2 ? nw2 : 0);
+    r.p2_partials = sc.take<uint64_t>(compact2 ? bitmap_prefix_partials(nw2) : 0);
+    r.p2_total = sc.take<uint64_t>(1);
     r.tot = sc.take<uint32_t>(4 * (uint64_t)B);
     r.seq_off_store = sc.take<uint64_t>(B + 1);
     r.tile_base = sc.take<uint64_t>(B + 1);
@@ -934,7 +970,8 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     // dense tables c1 | coff | c2 | tot are contiguous in scratch: zero what needs it
     if (!a.compact1) PHYLO_CHECK(cudaMemsetAsync(a.c1, 0, sizeof(uint32_t) * a.T1s * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.seen1, 0, sizeof(uint32_t) * (a.T1s / 32) * a.B, st));
-    PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
+    if (a.compact2) PHYLO_CHECK(cudaMemsetAsync(a.seen2, 0, sizeof(uint32_t) * (a.T2s / 32) * a.B, st));
+    else PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.T2 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.tot, 0, sizeof(uint32_t) * 4 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.status, 0, sizeof(uint32_t) * 4, st));
     k_prep<<<1, 32, 0, st>>>(a.B, a.seq_off, a.tile_base);
@@ -946,6 +983,13 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     } else {
         k_count<false><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
         PHYLO_CHECK(cudaMemsetAsync(a.p1_total, 0, sizeof(uint64_t), st));
+    }
+    if (a.compact2) {  // ranks of the seen (K-2)-mers; their counts (k_c0_scatter) start at 0
+        PHYLO_CHECK(bitmap_prefix_pairs(a.seen2, a.T2s / 32 * a.B, a.p2_partials, a.pw2,
+                                        a.p2_total, st));
+        PHYLO_CHECK(cudaMemsetAsync(a.c2, 0, sizeof(uint32_t) * a.cap2, st));
+    } else {
+        PHYLO_CHECK(cudaMemsetAsync(a.p2_total, 0, sizeof(uint64_t), st));
     }
     k_tables<<<dim3(PROB_TABLE / 256, a.B), 256, 0, st>>>(a);
     k_tuple_alpha<<<dim3(TUPLE_TABLE / 256, a.B), 256, 0, st>>>(a);

@@ -9,6 +9,7 @@ struct BuildGeometry {
     uint32_t A;      // alphabet size (21 protein, 4 DNA)
     uint64_t T1, T2; // A^(K-1), A^(K-2)
     uint64_t T1s;    // per-proteome row length of the (K-1)-mer tables (T1 rounded up to 32)
+    uint64_t T2s;    // the same for the (K-2)-mer tables
     uint64_t NCH;    // chunks of the seen bitmap per proteome (CHUNK_THREADS * wpt words)
     uint32_t wpt;    // bitmap words per thread in the candidate passes
 };
@@ -50,7 +51,7 @@ constexpr uint32_t TUPLE_TAG = 0xffff0000u;
 struct BuildArgs {
     int alpha, k, B;
     uint32_t A;
-    uint64_t T1, T2, T1s, NCH;
+    uint64_t T1, T2, T1s, T2s, NCH;
     uint32_t wpt;
     // input: concatenated sequences, seq_off[B+1] (device)
     const uint8_t *seq;
@@ -58,7 +59,7 @@ struct BuildArgs {
     uint64_t *seq_off_store;  // scratch home for seq_off of a single proteome
     uint64_t *tile_base;      // [B+1]
     // (K-1)-mer tables: dense [B][T1s] (coff written for seen (K-1)-mers only), or,
-    // when `compact1` (tables beyond 2^24 entries), one entry per seen (K-1)-mer of
+    // when `compact1` (tables beyond 2^20 entries), one entry per seen (K-1)-mer of
     // the batch, at its rank among the seen bits: pw1[word].x + popc(bits below)
     uint32_t *c1, *coff;
     int compact1;
@@ -67,7 +68,14 @@ struct BuildArgs {
     uint64_t *p1_partials, *p1_total;
     uint32_t *seen1;          // [B][T1s / 32]: bitmap of the seen (K-1)-mers
     uint32_t *word_cand;      // [B][T1s / 32]: candidates of each bitmap word
-    uint32_t *c2;             // [B][T2]
+    // (K-2)-mer counts: dense [B][T2], or, when `compact2` (beyond 2^20 entries),
+    // one entry per seen (K-2)-mer of the batch, at its rank in seen2 (via pw2)
+    uint32_t *c2;
+    int compact2;
+    uint64_t cap2;            // entries of c2 in compact mode
+    uint32_t *seen2;          // [B][T2s / 32]: bitmap of the seen (K-2)-mers (compact2)
+    uint2 *pw2;               // [B * T2s / 32]: {set bits of seen2 before the word, the word}
+    uint64_t *p2_partials, *p2_total;
     uint32_t *tot;            // [B][4]: n0, n1, n2, -
     // per (proteome, chunk of CH (K-1)-mers)
     uint32_t *chunk_cand;     // candidates per chunk

@@ -133,3 +133,30 @@ def test_batched_build_equals_single_and_counts():
                                           k1.ctypes.data, k2.ctypes.data, tot.ctypes.data))
     e1, e2, et = O.count_tables(p.get(5), 6)
     assert np.array_equal(k1, e1) and np.array_equal(k2, e2) and tuple(tot) == et
+
+
+def test_batched_counts_k7_compact_tables():
+    """Protein K = 7 keeps both the (K-1)- and the (K-2)-mer counts compact (one
+    entry per seen (K-1)- / (K-2)-mer of the batch); phyloBuildBatchCounts expands
+    them: both tables and the totals equal the oracle's dense ones."""
+    p = synth.workload("uneven1024", n=3, scale=0.03)
+    d = torch.from_numpy(p.data).cuda()
+    b = BatchBuilder("protein", 7, max_batch=2)  # two sub-batches
+    arena = b.build(d, p.offsets)
+    torch.cuda.synchronize()
+    for i in range(3):
+        r = O.cv_native(p.get(i), 7)
+        k, v = arena.host_vector(i)
+        assert np.array_equal(k, r["keys"])
+        assert ulp_diff(v, r["values"]) <= 1
+    L = _native.load()
+    scr = b._scratch[1] if b.overlap else b._scratch[0]
+    k1 = np.zeros(21 ** 6, np.uint32)
+    k2 = np.zeros(21 ** 5, np.uint32)
+    tot = np.zeros(3, np.uint32)
+    cand = int(np.sum(np.minimum(8 * p.lengths()[2:] + 65536, 21 ** 7)))
+    _native.check(L.phyloBuildBatchCounts(torch.cuda.current_stream().cuda_stream,
+                                          scr.data_ptr(), scr.numel(), b"protein", 7, 1, cand, 0,
+                                          k1.ctypes.data, k2.ctypes.data, tot.ctypes.data))
+    e1, e2, et = O.count_tables(p.get(2), 7)
+    assert np.array_equal(k1, e1) and np.array_equal(k2, e2) and tuple(tot) == et
