@@ -147,6 +147,7 @@ class BatchBuilder:
         self._scratch = [None, None]
         self._summary = [None, None]
         self._side = None
+        self._copy = None  # stream of the per-batch residue copies (build(host=...))
         self.launches = 0
 
     def _scratch_for(self, slot: int, B: int, cand_cap: int) -> torch.Tensor:
@@ -174,10 +175,16 @@ class BatchBuilder:
                      np.zeros(1, np.int64), np.zeros(0, np.float64))
 
     def build(self, seq: torch.Tensor, seq_off: np.ndarray, arena: Optional[Arena] = None,
-              stream: Optional[torch.cuda.Stream] = None) -> Arena:
+              stream: Optional[torch.cuda.Stream] = None,
+              host: Optional[torch.Tensor] = None) -> Arena:
         """Builds the proteomes seq[seq_off[i]:seq_off[i+1]] (seq on the device) and
         appends them to ``arena`` (a new one if None).  Work is ordered on ``stream``
-        (default: the current stream): later work on it sees the whole build."""
+        (default: the current stream): later work on it sees the whole build.
+
+        ``host``: the same residues in pinned host memory.  Each batch's range is then
+        copied into ``seq`` on a copy stream just ahead of the batch, so the copies of
+        later batches overlap the build of earlier ones (the pinned, double-buffered
+        ingest of DeviceWorker.java:118-157)."""
         seq_off = np.asarray(seq_off, np.int64)
         n = len(seq_off) - 1
         lens = np.diff(seq_off)
@@ -186,14 +193,22 @@ class BatchBuilder:
         if arena.vec_off.numel() < arena.n + n + 1:
             arena.vec_off = _grow(arena.vec_off, arena.n + n + 1)
         s_obj = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if host is not None and (host.device.type != "cpu" or host.numel() < seq_off[-1]):
+            raise ValueError("host residues: a CPU tensor covering seq_off")
         with torch.cuda.stream(s_obj):
-            self._build_into(arena, seq, seq_off, lens, s_obj)
+            self._build_into(arena, seq, seq_off, lens, s_obj, host)
         return arena
 
     def _build_into(self, arena: Arena, seq: torch.Tensor, seq_off: np.ndarray, lens: np.ndarray,
-                    stream: torch.cuda.Stream) -> None:
+                    stream: torch.cuda.Stream, host: Optional[torch.Tensor] = None) -> None:
         n = len(seq_off) - 1
         d_seq_off_all = torch.from_numpy(seq_off).to(self.device, non_blocking=False)
+        if host is not None:  # copies wait for earlier work on the stream (it may read seq)
+            if self._copy is None:
+                self._copy = torch.cuda.Stream(self.device)
+            ready = torch.cuda.Event()
+            ready.record(stream)
+            self._copy.wait_event(ready)
         batches = [(f, min(self.max_batch, n - f)) for f in range(0, n, self.max_batch)]
         overlap = self.overlap and len(batches) > 1
         streams = [stream]
@@ -213,10 +228,17 @@ class BatchBuilder:
             lens_b = lens[first:first + B]
             cand = int(np.sum(np.minimum(8 * lens_b + 65536, key_limit(self.alphabet, self.k))))
             base = int(seq_off[first])
+            end = int(seq_off[first + B])
+            if host is not None and end > base:  # this batch's residues, ahead of its build
+                with torch.cuda.stream(self._copy):
+                    seq[base:end].copy_(host[base:end], non_blocking=True)
+                copied = torch.cuda.Event()
+                copied.record(self._copy)
+                st.wait_event(copied)
             with torch.cuda.stream(st):
                 d_off = d_seq_off_all[first:first + B + 1] - base
                 scr = self._scratch_for(slot, B, cand)
-            d_seq = seq[base:int(seq_off[first + B])]
+            d_seq = seq[base:end]
             keep.append(d_off)
             summ = self._summary_for(slot)
             check(self.L.phyloBuildBatchPlanAsync(

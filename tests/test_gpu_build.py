@@ -160,3 +160,22 @@ def test_batched_counts_k7_compact_tables():
                                           k1.ctypes.data, k2.ctypes.data, tot.ctypes.data))
     e1, e2, et = O.count_tables(p.get(2), 7)
     assert np.array_equal(k1, e1) and np.array_equal(k2, e2) and tuple(tot) == et
+
+
+def test_build_from_pinned_host_residues():
+    """build(host=...) copies each batch's residues from pinned memory just ahead of
+    the batch (the copies overlap earlier batches); the arena equals a build from
+    residues already on the device, also when the device buffer held other data."""
+    p = synth.workload("uneven1024", n=7, scale=0.03)
+    b1 = BatchBuilder("protein", 6, max_batch=3)
+    ref = b1.build(torch.from_numpy(p.data).cuda(), p.offsets)
+    pinned = torch.from_numpy(p.data).pin_memory()
+    seq = torch.full((p.data.size,), ord("W"), dtype=torch.uint8, device="cuda")
+    b2 = BatchBuilder("protein", 6, max_batch=3)
+    got = b2.build(seq, p.offsets, host=pinned)
+    torch.cuda.synchronize()
+    assert got.n == ref.n == 7
+    for i in range(7):
+        k1, v1 = ref.host_vector(i)
+        k2, v2 = got.host_vector(i)
+        assert np.array_equal(k1, k2) and np.array_equal(v1, v2)
