@@ -203,13 +203,16 @@ class BatchBuilder:
                     stream: torch.cuda.Stream, host: Optional[torch.Tensor] = None) -> None:
         n = len(seq_off) - 1
         d_seq_off_all = torch.from_numpy(seq_off).to(self.device, non_blocking=False)
+        batches = [(f, min(self.max_batch, n - f)) for f in range(0, n, self.max_batch)]
+        if host is not None and len(batches) == 1:  # nothing to overlap: one copy, in order
+            seq[:int(seq_off[-1])].copy_(host[:int(seq_off[-1])], non_blocking=True)
+            host = None
         if host is not None:  # copies wait for earlier work on the stream (it may read seq)
             if self._copy is None:
                 self._copy = torch.cuda.Stream(self.device)
             ready = torch.cuda.Event()
             ready.record(stream)
             self._copy.wait_event(ready)
-        batches = [(f, min(self.max_batch, n - f)) for f in range(0, n, self.max_batch)]
         overlap = self.overlap and len(batches) > 1
         streams = [stream]
         if overlap:

@@ -175,7 +175,12 @@ def test_build_from_pinned_host_residues():
     got = b2.build(seq, p.offsets, host=pinned)
     torch.cuda.synchronize()
     assert got.n == ref.n == 7
+    # one batch: a single copy, ordered before the build on its stream
+    seq1 = torch.full((p.data.size,), ord("W"), dtype=torch.uint8, device="cuda")
+    one = BatchBuilder("protein", 6, max_batch=24).build(seq1, p.offsets, host=pinned)
+    torch.cuda.synchronize()
     for i in range(7):
         k1, v1 = ref.host_vector(i)
-        k2, v2 = got.host_vector(i)
-        assert np.array_equal(k1, k2) and np.array_equal(v1, v2)
+        for arena in (got, one):
+            k2, v2 = arena.host_vector(i)
+            assert np.array_equal(k1, k2) and np.array_equal(v1, v2)
