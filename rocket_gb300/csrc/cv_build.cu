@@ -568,8 +568,8 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
 // (native.cu:392 with p = 0) and needs no table loads.  The others are listed
 // per warp in shared memory and computed densely, 32 lanes on 32 of them, so
 // the long path does not run with most lanes idle.
-constexpr int ALPHA_ILP = 2;  // listed candidates per lane in flight together
-__global__ void __launch_bounds__(CHUNK_THREADS, 5) k_alpha(BuildArgs a) {
+constexpr int ALPHA_ILP = 1;  // listed candidates per lane in flight together
+__global__ void __launch_bounds__(CHUNK_THREADS, 6) k_alpha(BuildArgs a) {
     __shared__ U192 s_norm[CHUNK_THREADS / 32];
     __shared__ uint32_t s_m1[CHUNK_THREADS / 32], s_bad[CHUNK_THREADS / 32];
     __shared__ uint32_t s_key[CHUNK_THREADS / 32][SEG];    // keys by segment index
