@@ -398,6 +398,8 @@ class PairEngine:
         self.launches = 0
         self.cmp_scratch = None
         self.self_part = None
+        self._rank_scratch = None
+        self._rank_marked = False  # the last rank prefix used the build's union bitmap
 
     # -- window index ------------------------------------------------------
     def ensure_index(self, stream=None) -> None:
@@ -446,7 +448,7 @@ class PairEngine:
         union size; the ranks themselves come with the window index."""
         limit = key_limit(a.alphabet, a.k)
         nb = int(self.L.phyloKeyRankScratch(limit))
-        if getattr(self, "_rank_scratch", None) is None or self._rank_scratch.numel() < nb:
+        if self._rank_scratch is None or self._rank_scratch.numel() < nb:
             self._rank_scratch = torch.empty(nb, dtype=torch.uint8, device=self.device)
         if a.rkeys is None or a.rkeys.numel() < a.keys.numel():
             a.rkeys = torch.empty(a.keys.numel(), dtype=torch.int32, device=self.device)
