@@ -74,14 +74,15 @@ int compareCompositionVectors(uintptr_t stream, uintptr_t d_temp_storage_ptr, lo
  * device memory into fixed cache slots at start-up (Rocket's device cache works
  * this way) and has no spare buffer for scratch, or a caller whose device
  * memory is owned by another framework's allocator.  This entry point takes no
- * scratch argument and allocates nothing: the compare kernels use a fixed-size
- * array built into the library (about 73 KB, present on every GPU that loads the
+ * scratch argument and allocates nothing: the compare kernel uses a fixed-size
+ * array built into the library (8,448 bytes, present on every GPU that loads the
  * library until the process exits).  The caller still passes the inputs and the
  * output (one double, device memory).
  *
  * Limit: left_size + right_size <= 67,108,864 (2^26); larger inputs are refused
  * with cudaErrorInvalidValue and a message, before any kernel runs.
- * The first call on each device looks up the array's device address
+ * The first call in each CUDA context (one per device, or one per context the
+ * caller creates) looks up the array's device address in that context
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * All calls share the one array: calls whose kernels could overlap on the GPU
  * (other streams, other host threads) must be serialised by the caller.
@@ -91,6 +92,17 @@ int compareCompositionVectorsStatic(uintptr_t stream, uintptr_t d_left_keys_ptr,
                                     uintptr_t d_left_values_ptr, int left_size,
                                     uintptr_t d_right_keys_ptr, uintptr_t d_right_values_ptr,
                                     int right_size, uintptr_t d_output_ptr);
+
+/*
+ * Test hook of the compare kernels' bounded waits (no counterpart in the
+ * reference).  Every mbarrier wait of the compare kernels gives up after a poll
+ * limit, records DEV_WAIT_TIMEOUT in the status word, waits (bounded) for its
+ * own copies in flight and returns; the synchronous entry points then return
+ * cudaErrorLaunchTimeout (702).  This sets the limit of each CTA's first wait
+ * (0 = give up at once; 0xffffffff restores the default of 2^22 polls), so that
+ * a test can take that path without a fault.  Process-wide; not for production.
+ */
+void phyloCompareTestWaitLimit(unsigned int limit);
 
 /* ---------------------------------------------------------------------------
  * Batched construction (new; the reference builds one proteome per call,
@@ -216,6 +228,50 @@ int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int 
 
 /* Scratch bytes phyloSelfDot needs. */
 long phyloSelfDotPartBytes(int num_vectors, long max_vector_len);
+
+/* Key-major (postings) pair engine.  Replaces, for a whole set of pairs, the
+ * per-pair merge path of native.cu:541-703 (one compareCompositionVectors per
+ * pair, DeviceWorker.submitCorrelation, DeviceWorker.java:237-323): a work item
+ * is a block of row vectors x a block of column vectors (block = 128 or 64) over
+ * a run of key windows; each window's entries are regrouped by key in shared
+ * memory and only the products of shared keys are formed.  Products are rounded
+ * once to a multiple of 2^-46 and summed exactly in 64-bit integers, so C is
+ * within (products) * 2^-47 of the exact value and independent of scheduling.
+ * Values must satisfy |v| < 2^7 (normalised vectors do); non-finite values count
+ * as 0 (recompute those pairs with phyloComparePairsMany).
+ *
+ * Capacity: posting entries per side that one chunk of a window holds; -1 for
+ * an unsupported block / window shift (4..14).  Prepare sets the kernel's
+ * shared-memory limit in the current context and reports resident CTAs per SM. */
+long phyloPostingsSmemBytes(int block, int window_shift);
+long phyloPostingsCapacity(int block, int window_shift);
+int phyloPostingsThreads(int block);
+int phyloPostingsPrepare(int block, int window_shift, int *ctas_per_sm);
+
+/* Work items: 8 uint32 each (row0, nrow, col0, ncol, w0, w1, part, diag); rows
+ * are positions in d_rowids, columns in d_colids; diag = 1 when the rows and the
+ * columns are the same block (each unordered pair and self product once).  Each
+ * item writes block x block int64 partial sums (units of 2^-46) at d_part + part *
+ * block^2 * 8 bytes.  d_counter (uint32) must be 0; d_status (uint32, may be 0)
+ * receives DeviceError bits (2: an entry outside its window, 4: a value out of
+ * range); d_item_cycles (int64[num_items], may be 0) per-item clock64 durations.
+ * The window index (d_roff) and keys are those of phyloWindowIndex /
+ * phyloKeyRankIndex.  Asynchronous. */
+int phyloPostingsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_values,
+                        uintptr_t d_row_vec_off, uintptr_t d_row_roff, uintptr_t d_col_keys,
+                        uintptr_t d_col_values, uintptr_t d_col_vec_off, uintptr_t d_col_roff,
+                        unsigned int num_windows, int window_shift, uintptr_t d_rowids,
+                        uintptr_t d_colids, uintptr_t d_items, int num_items, uintptr_t d_counter,
+                        uintptr_t d_part, uintptr_t d_status, uintptr_t d_item_cycles, int block,
+                        int grid);
+
+/* Sums each tile's partials (tiles: 8 uint32 each: row0, nrow, col0, ncol, part0,
+ * nparts, diag, 0) in a fixed order into d_out[rowid * ldc + colid] (double); in a
+ * diag tile the pairs of row position < column position, and with `self` the self
+ * products too; `mirror` also writes the transposed entry.  Asynchronous. */
+int phyloPostingsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
+                        int block, uintptr_t d_rowids, uintptr_t d_colids, uintptr_t d_out,
+                        long ldc, int self, int mirror);
 
 /* Dense key ranks (no counterpart in the reference: an input transform of
  * the batched pair path).  d_rank_keys[e] = number of distinct keys of the

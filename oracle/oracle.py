@@ -150,16 +150,71 @@ def cv_native(seq, k: int, alphabet: str = "protein", formulation: str = "candid
     return out
 
 
+def exact_sum_of_floats(x: np.ndarray) -> float:
+    """The correctly rounded double of the exact sum of float32 values.
+
+    Every finite float32 is m * 2^(e - 150) with an integer significand m < 2^24
+    and biased exponent e (1 for subnormals).  The significands are summed per
+    exponent in two 12-bit halves -- each half-sum stays below 2^53 for up to
+    2^41 values, so the float64 bin counts are exact -- and the 2 x 256 exact
+    partial sums are added by math.fsum, which rounds once."""
+    x = np.ascontiguousarray(x, np.float32)
+    if len(x) == 0:
+        return 0.0
+    if not np.all(np.isfinite(x)):
+        return float(np.sum(x.astype(np.float64)))  # inf / nan propagate
+    b = x.view(np.uint32)
+    terms = []
+    negative = b >> 31
+    for sign, part in ((1.0, b), (-1.0, None)):
+        if part is None:
+            if not negative.any():
+                break
+            part = b[negative.astype(bool)]
+        elif negative.any():
+            part = b[~negative.astype(bool)]
+        e = (part >> 23) & 0xFF          # biased exponent (sign bit cleared)
+        m = part & 0x7FFFFF
+        m = m | ((e > 0).astype(np.uint32) << 23)  # the implicit bit of normal numbers
+        e = np.maximum(e, 1)
+        lo = np.bincount(e, weights=m & 0xFFF, minlength=256)
+        hi = np.bincount(e, weights=m >> 12, minlength=256)
+        for k in np.flatnonzero(lo):
+            terms.append(sign * math.ldexp(lo[k], int(k) - 150))
+        for k in np.flatnonzero(hi):
+            terms.append(sign * math.ldexp(hi[k], int(k) - 138))
+    return math.fsum(terms)
+
+
 def normalise(alpha: np.ndarray):
     """norm = exact sum of float(f*f) (native.cu:415-428, summed exactly);
     values = float(double(f) / sqrt(norm)) (native.cu:460-468)."""
     f = np.asarray(alpha, np.float32)
-    sq = (f * f).astype(np.float64)  # float product, as the reference's lambda
-    norm = math.fsum(sq.tolist()) if len(sq) else 0.0
+    sq = f * f  # float product, as the reference's lambda
+    norm = exact_sum_of_floats(sq)
     with np.errstate(invalid="ignore", divide="ignore"):
         values = (f.astype(np.float64) / math.sqrt(norm)).astype(np.float32) if len(f) else \
             np.zeros(0, np.float32)
     return norm, values
+
+
+def digest(keys: np.ndarray, values: np.ndarray):
+    """(size, key digest, value digest): order-sensitive 64-bit sums over a vector,
+    sum (key_i + 1)(2 i + 1) and sum (bits(value_i) + 7)(i + 3), wrapping mod 2^64."""
+    k = np.asarray(keys, np.uint32).astype(np.uint64)
+    v = np.asarray(values, np.float32).view(np.uint32).astype(np.uint64)
+    i = np.arange(len(k), dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        hk = int(np.sum((k + np.uint64(1)) * (np.uint64(2) * i + np.uint64(1)), dtype=np.uint64))
+        hv = int(np.sum((v + np.uint64(7)) * (i + np.uint64(3)), dtype=np.uint64))
+    return len(k), hk, hv
+
+
+def cv_native_digest(args):
+    """digest() of cv_native(seq, k) -- for a worker pool (no large arrays back)."""
+    seq, k = args
+    r = cv_native(seq, k)
+    return digest(r["keys"], r["values"])
 
 
 def count_tables(seq, k: int, alphabet: str = "protein"):

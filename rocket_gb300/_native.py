@@ -63,6 +63,8 @@ def _declare(L: ctypes.CDLL) -> None:
     L.compareCompositionVectorsStatic.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_ptr, c_ptr, c_int,
                                                   c_ptr]
     L.compareCompositionVectorsStatic.restype = c_int
+    L.phyloCompareTestWaitLimit.argtypes = [c_uint]
+    L.phyloCompareTestWaitLimit.restype = None
     # batched construction
     L.phyloBuildBatchScratch.argtypes = [c_char_p, c_int, c_int, c_long]
     L.phyloBuildBatchScratch.restype = c_long
@@ -121,12 +123,27 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloComparePairsManyScratch.restype = c_long
     L.phyloComparePairsMany.argtypes = [c_ptr, c_ptr, c_long] + [c_ptr] * 10 + [c_int, c_long, c_ptr]
     L.phyloComparePairsMany.restype = c_int
+    # key-major (postings) pair engine
+    L.phyloPostingsSmemBytes.argtypes = [c_int, c_int]
+    L.phyloPostingsSmemBytes.restype = c_long
+    L.phyloPostingsCapacity.argtypes = [c_int, c_int]
+    L.phyloPostingsCapacity.restype = c_long
+    L.phyloPostingsThreads.argtypes = [c_int]
+    L.phyloPostingsThreads.restype = c_int
+    L.phyloPostingsPrepare.argtypes = [c_int, c_int, ctypes.POINTER(c_int)]
+    L.phyloPostingsPrepare.restype = c_int
+    L.phyloPostingsLaunch.argtypes = [c_ptr] * 9 + [c_uint, c_int] + [c_ptr] * 3 + [c_int] + \
+        [c_ptr] * 4 + [c_int, c_int]
+    L.phyloPostingsLaunch.restype = c_int
+    L.phyloPostingsReduce.argtypes = [c_ptr, c_ptr, c_ptr, c_int, c_int, c_ptr, c_ptr, c_ptr,
+                                      c_long, c_int, c_int]
+    L.phyloPostingsReduce.restype = c_int
 
 
 # Every symbol that include/phylogenetics.h declares.
 EXPORTED = [
     "estimateScratchMemory", "buildCompositionVector", "compareCompositionVectors",
-    "compareCompositionVectorsStatic", "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchPlanAsync",
+    "compareCompositionVectorsStatic", "phyloCompareTestWaitLimit", "phyloBuildBatchScratch", "phyloBuildBatchPlan", "phyloBuildBatchPlanAsync",
     "phyloBuildBatchSummaryBytes", "phyloBuildBatchEmit", "phyloBuildBatchNorms",
     "phyloBuildBatchCounts", "phyloBuildLaunchesPerBatch", "phyloWindowIndex",
     "phyloPairsPrepare", "phyloPairsSmemBytes", "phyloPairsThreads", "phyloPairsLaunch",
@@ -135,11 +152,13 @@ EXPORTED = [
     "phyloKeyRanks", "phyloKeyRankIndex",
     "phyloComparePairsManyScratch",
     "phyloComparePairsMany", "phyloComparePairAsync",
+    "phyloPostingsSmemBytes", "phyloPostingsCapacity", "phyloPostingsThreads",
+    "phyloPostingsPrepare", "phyloPostingsLaunch", "phyloPostingsReduce",
 ]
 
 
 CUDA_ERROR_NAMES = {0: "cudaSuccess", 1: "cudaErrorInvalidValue", 2: "cudaErrorMemoryAllocation",
-                    6: "cudaErrorLaunchTimeout", 999: "cudaErrorUnknown"}
+                    702: "cudaErrorLaunchTimeout", 999: "cudaErrorUnknown"}
 
 
 class CudaException(RuntimeError):

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphylogenetics.so")
 SYNTH_LIB = os.path.join(HERE, "libphylo_synth.so")
-SOURCES = ["cv_build.cu", "compare.cu", "allpairs.cu", "rank.cu", "capi.cu"]
+SOURCES = ["cv_build.cu", "compare.cu", "allpairs.cu", "postings.cu", "rank.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2"]
 

@@ -25,6 +25,7 @@
 #include "allpairs.cuh"
 #include "compare.cuh"
 #include "cv_build.cuh"
+#include "postings.cuh"
 #include "rank.cuh"
 
 using namespace phylo;
@@ -230,6 +231,9 @@ int compareCompositionVectorsStatic(uintptr_t stream, uintptr_t d_left_keys_ptr,
     }
     return (int)cudaGetLastError();
 }
+
+// Test hook of the bounded waits (see include/phylogenetics.h).
+void phyloCompareTestWaitLimit(unsigned int limit) { compare_set_first_wait_limit(limit); }
 
 // ---------------------------------------------------------------------------
 // batched construction (new)
@@ -524,6 +528,79 @@ int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int 
     r.upper = upper;
     r.mirror = mirror;
     return (int)ap_reduce_launch(r, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// key-major (postings) pair engine (new)
+// ---------------------------------------------------------------------------
+
+long phyloPostingsSmemBytes(int block, int window_shift) {
+    if (!pb_block_ok(block) || window_shift < 4 || window_shift > 14) return -1;
+    const size_t n = pb_smem_bytes(block, (uint32_t)window_shift);
+    return n ? (long)n : -1;
+}
+
+long phyloPostingsCapacity(int block, int window_shift) {
+    if (!pb_block_ok(block) || window_shift < 4 || window_shift > 14) return -1;
+    const uint32_t c = pb_capacity(block, (uint32_t)window_shift);
+    return c ? (long)c : -1;
+}
+
+int phyloPostingsThreads(int block) { return pb_block_ok(block) ? pb_threads(block) : -1; }
+
+int phyloPostingsPrepare(int block, int window_shift, int *ctas_per_sm) {
+    if (phyloPostingsCapacity(block, window_shift) < 0) return (int)cudaErrorInvalidValue;
+    return (int)pb_prepare(block, (uint32_t)window_shift, ctas_per_sm);
+}
+
+int phyloPostingsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_values,
+                        uintptr_t d_row_vec_off, uintptr_t d_row_roff, uintptr_t d_col_keys,
+                        uintptr_t d_col_values, uintptr_t d_col_vec_off, uintptr_t d_col_roff,
+                        unsigned int num_windows, int window_shift, uintptr_t d_rowids,
+                        uintptr_t d_colids, uintptr_t d_items, int num_items, uintptr_t d_counter,
+                        uintptr_t d_part, uintptr_t d_status, uintptr_t d_item_cycles, int block,
+                        int grid) {
+    if (phyloPostingsCapacity(block, window_shift) < 0 || num_items < 0 || grid <= 0)
+        return (int)cudaErrorInvalidValue;
+    if (num_items == 0) return 0;
+    PbArgs a;
+    a.row.keys = (const uint32_t *)d_row_keys;
+    a.row.vals = (const float *)d_row_values;
+    a.row.vec_off = (const uint64_t *)d_row_vec_off;
+    a.row.roff = (const uint32_t *)d_row_roff;
+    a.col.keys = (const uint32_t *)d_col_keys;
+    a.col.vals = (const float *)d_col_values;
+    a.col.vec_off = (const uint64_t *)d_col_vec_off;
+    a.col.roff = (const uint32_t *)d_col_roff;
+    a.R = num_windows;
+    a.wshift = (uint32_t)window_shift;
+    a.rowids = (const uint32_t *)d_rowids;
+    a.colids = (const uint32_t *)d_colids;
+    a.items = (const PbItem *)d_items;
+    a.nitems = (uint32_t)num_items;
+    a.counter = (uint32_t *)d_counter;
+    a.part = (int64_t *)d_part;
+    a.status = (uint32_t *)d_status;
+    a.item_cycles = (int64_t *)d_item_cycles;
+    return (int)pb_launch(a, block, grid, (cudaStream_t)stream);
+}
+
+int phyloPostingsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
+                        int block, uintptr_t d_rowids, uintptr_t d_colids, uintptr_t d_out,
+                        long ldc, int self, int mirror) {
+    if (!pb_block_ok(block) || num_tiles < 0 || ldc <= 0) return (int)cudaErrorInvalidValue;
+    PbReduceArgs r;
+    r.part = (const int64_t *)d_part;
+    r.tiles = (const PbTile *)d_tiles;
+    r.ntiles = (uint32_t)num_tiles;
+    r.block = (uint32_t)block;
+    r.rowids = (const uint32_t *)d_rowids;
+    r.colids = (const uint32_t *)d_colids;
+    r.out = (double *)d_out;
+    r.ldc = (uint64_t)ldc;
+    r.self = self;
+    r.mirror = mirror;
+    return (int)pb_reduce_launch(r, (cudaStream_t)stream);
 }
 
 long phyloKeyRankScratch(long key_limit) {

@@ -34,6 +34,7 @@ enum DeviceError : uint32_t {
     DEV_OK = 0,
     DEV_WAIT_TIMEOUT = 1,     // an mbarrier wait exceeded its iteration limit
     DEV_CAPACITY = 2,         // an output/staging capacity was exceeded
+    DEV_RANGE = 4,            // an input value outside the range a kernel accepts
 };
 
 // ------------------------------------------------------------------------

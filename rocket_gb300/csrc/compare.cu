@@ -1,29 +1,30 @@
-// compare.cu -- sparse cosine of one pair of composition vectors.
+// compare.cu -- sparse cosine of one pair (and of many pairs) of composition vectors.
 //
 // C = sum over keys present in both lists of a * b, the quantity the reference
 // computes with a merge-path partition and one merge step per thread
-// (phylogenetics/src/main/cpp/native.cu:513-703).  This version:
+// (phylogenetics/src/main/cpp/native.cu:513-703).  This version is one launch:
 //
-//   * k_partition: one warp per tile boundary finds the merge-path split of
-//     diagonal t*TILE by a 32-ary search (about five dependent global loads
-//     instead of twenty), ties going to the left list as in native.cu:529.
-//     It also resets the completion ticket and the status word.
-//   * k_intersect: persistent CTAs walk contiguous runs of tiles.  For each
-//     tile a single thread issues 1-D bulk copies (TMA) of the left and right
-//     key/value ranges into shared memory, double-buffered on mbarriers; all
-//     threads then run a per-thread merge-path over 16 diagonals in shared
-//     memory.  Products are split exactly (TwoProduct) and summed as
-//     float-float (TwoSum); warp shuffles and one shared-memory step reduce
-//     the CTA, and the last CTA combines the per-CTA partials in a fixed
+//   * k_compare: persistent CTAs take contiguous runs of tiles of 4096 merged
+//     elements.  Each CTA first finds the merge-path splits of its own tile
+//     boundaries, one warp per boundary by a 32-ary search (about five dependent
+//     global loads instead of twenty), ties going to the left list as in
+//     native.cu:529.  Then, for each tile, a single thread issues 1-D bulk copies
+//     (TMA) of the left and right key/value ranges into shared memory,
+//     double-buffered on mbarriers; all threads run a per-thread merge path over
+//     16 diagonals in shared memory.  Products are split exactly (TwoProduct) and
+//     summed as float-float (TwoSum); warp shuffles and one shared-memory step
+//     reduce the CTA, and the last CTA combines the per-CTA partials in a fixed
 //     order into the double result.
+//   * k_many_intersect does the same over the tiles of many pairs in one index
+//     space; each CTA resolves its tiles' pairs, vector offsets and splits up
+//     front, so issuing a tile's copies reads only shared memory.
 //
 // Ranges need not be 16-byte aligned: each copy is widened to 16-byte
 // boundaries (never leaving the 16-byte block of a valid element) and the
 // consumer indexes from the offset.
 #include "compare.cuh"
+#include "hostctx.cuh"
 #include "scan.cuh"
-
-#include <mutex>
 
 namespace phylo {
 
@@ -31,18 +32,29 @@ constexpr int CMP_THREADS = 256;
 constexpr int CMP_IPT = 16;
 constexpr int CMP_TILE = CMP_THREADS * CMP_IPT;  // merged elements per tile
 constexpr int CMP_BUF = CMP_TILE + 20;           // entries per stage per type (A + B + look-ahead)
-constexpr int CMP_MAX_CTAS = 1024;
+constexpr uint32_t CMP_MAX_RUN = 64;             // tiles per CTA at most
+constexpr uint32_t CMP_MIN_CAP = 1024;           // partial slots always carved
 
+// Completion ticket and status first (cleared before every launch), then one
+// float-float partial per CTA.
 struct CmpState {
-    FF partial[CMP_MAX_CTAS];
     uint32_t ticket;
     uint32_t status;
+    uint32_t pad[2];
+    FF partial[1];  // [cmp_partials(ntiles)]
 };
 
-size_t compare_scratch_bytes(uint64_t max_total) {
-    uint64_t ntiles = div_up(max_total, CMP_TILE) + 1;
-    return scratch_bytes<uint32_t>(ntiles + 1) + scratch_bytes<CmpState>(1);
+__host__ __device__ constexpr uint64_t cmp_partials(uint64_t ntiles) {
+    return (ntiles + CMP_MAX_RUN - 1) / CMP_MAX_RUN > CMP_MIN_CAP
+               ? (ntiles + CMP_MAX_RUN - 1) / CMP_MAX_RUN
+               : CMP_MIN_CAP;
 }
+
+__host__ __device__ constexpr size_t cmp_state_bytes(uint64_t max_total) {
+    return (16 + 8 * cmp_partials((max_total + CMP_TILE - 1) / CMP_TILE) + 255) / 256 * 256;
+}
+
+size_t compare_scratch_bytes(uint64_t max_total) { return cmp_state_bytes(max_total); }
 
 // i = number of left elements before merged position d (ties to the left list).
 __device__ __forceinline__ uint32_t warp_merge_path(uint64_t d, const uint32_t *__restrict__ A,
@@ -64,22 +76,6 @@ __device__ __forceinline__ uint32_t warp_merge_path(uint64_t d, const uint32_t *
         hi = nhi < hi ? (uint32_t)nhi : hi;
     }
     return lo;
-}
-
-__global__ void k_partition(const uint32_t *__restrict__ A, uint32_t na,
-                            const uint32_t *__restrict__ B, uint32_t nb, uint32_t ntiles,
-                            uint32_t *splits, CmpState *st) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        st->ticket = 0;
-        st->status = 0;
-    }
-    const uint32_t t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-    if (t > ntiles) return;
-    uint64_t d = (uint64_t)t * CMP_TILE;
-    const uint64_t total = (uint64_t)na + nb;
-    if (d > total) d = total;
-    const uint32_t i = warp_merge_path(d, A, na, B, nb);
-    if ((threadIdx.x & 31) == 0) splits[t] = i;
 }
 
 struct Stage {
@@ -124,14 +120,15 @@ __device__ __forceinline__ Stage issue_ranges(const uint32_t *Ak, const float *A
     return s;
 }
 
-// Issues the bulk copies of tile `t` of one pair into a stage buffer.
-__device__ __forceinline__ Stage issue_tile(uint32_t t, const uint32_t *splits, uint64_t total,
-                                            uint32_t nb_total, const uint32_t *Ak, const float *Av,
-                                            const uint32_t *Bk, const float *Bv, uint32_t *sk,
-                                            float *sv, uint64_t *bar, bool issue) {
+// Issues the bulk copies of tile `t` of one pair into a stage buffer; split[]
+// holds the left split of tiles t_begin .. t_end (shared memory).
+__device__ __forceinline__ Stage issue_tile(uint32_t t, uint32_t t_begin, const uint32_t *split,
+                                            uint64_t total, uint32_t nb_total, const uint32_t *Ak,
+                                            const float *Av, const uint32_t *Bk, const float *Bv,
+                                            uint32_t *sk, float *sv, uint64_t *bar, bool issue) {
     const uint64_t d0 = (uint64_t)t * CMP_TILE;
     const uint64_t d1 = min(d0 + CMP_TILE, total);
-    const uint32_t i0 = splits[t], i1 = splits[t + 1];
+    const uint32_t i0 = split[t - t_begin], i1 = split[t - t_begin + 1];
     const uint32_t j0 = (uint32_t)(d0 - i0), j1 = (uint32_t)(d1 - i1);
     // A match whose left element ends this tile can have its equal right element
     // start the next one (ties go left), so one right element past the tile is
@@ -174,10 +171,10 @@ __device__ __forceinline__ void merge_tile(const Stage &s, const uint32_t *skb, 
     }
 }
 
-__global__ void __launch_bounds__(CMP_THREADS) k_intersect(
+__global__ void __launch_bounds__(CMP_THREADS) k_compare(
     const uint32_t *__restrict__ Ak, const float *__restrict__ Av, uint32_t na,
-    const uint32_t *__restrict__ Bk, const float *__restrict__ Bv, uint32_t nb,
-    const uint32_t *__restrict__ splits, uint32_t ntiles, CmpState *st, double *out) {
+    const uint32_t *__restrict__ Bk, const float *__restrict__ Bv, uint32_t nb, uint32_t ntiles,
+    uint32_t per, uint32_t first_wait_limit, CmpState *st, double *out) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     uint32_t *sk[2];
     float *sv[2];
@@ -187,14 +184,22 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
     sv[1] = (float *)(sk[1] + CMP_BUF);
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ FF warp_part[CMP_THREADS / 32];
+    __shared__ uint32_t s_split[CMP_MAX_RUN + 1];
     __shared__ bool s_last;
     __shared__ bool s_fail;
 
     const uint64_t total = (uint64_t)na + nb;
-    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
     const uint32_t t_begin = blockIdx.x * per;
     const uint32_t t_end = min(ntiles, t_begin + per);
 
+    // merge-path splits of this CTA's tile boundaries t_begin .. t_end, a warp each
+    const uint32_t warp = threadIdx.x >> 5;
+    for (uint32_t b = warp; t_begin < t_end && b <= t_end - t_begin; b += CMP_THREADS / 32) {
+        uint64_t d = (uint64_t)(t_begin + b) * CMP_TILE;
+        if (d > total) d = total;
+        const uint32_t i = warp_merge_path(d, Ak, na, Bk, nb);
+        if ((threadIdx.x & 31) == 0) s_split[b] = i;
+    }
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -207,16 +212,17 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
     Stage stg0 = {0, 0, 0, 0, 0, 0, 0}, stg1 = {0, 0, 0, 0, 0, 0, 0};
     // prologue: tiles t_begin, t_begin+1
     if (t_begin < t_end)
-        stg0 = issue_tile(t_begin, splits, total, nb, Ak, Av, Bk, Bv, sk[0], sv[0], &bar[0],
-                          threadIdx.x == 0);
+        stg0 = issue_tile(t_begin, t_begin, s_split, total, nb, Ak, Av, Bk, Bv, sk[0], sv[0],
+                          &bar[0], threadIdx.x == 0);
     if (t_begin + 1 < t_end)
-        stg1 = issue_tile(t_begin + 1, splits, total, nb, Ak, Av, Bk, Bv, sk[1], sv[1], &bar[1],
-                          threadIdx.x == 0);
+        stg1 = issue_tile(t_begin + 1, t_begin, s_split, total, nb, Ak, Av, Bk, Bv, sk[1], sv[1],
+                          &bar[1], threadIdx.x == 0);
     uint32_t fail_at = 0xffffffffu;
     for (uint32_t t = t_begin; t < t_end; t++) {
         const int b = (t - t_begin) & 1;
         const uint32_t phase = ((t - t_begin) >> 1) & 1;
-        if (!mbar_wait_bounded(&bar[b], phase)) s_fail = true;
+        const uint32_t limit = t == t_begin ? first_wait_limit : (1u << 22);
+        if (!mbar_wait_bounded(&bar[b], phase, limit)) s_fail = true;
         __syncthreads();
         if (s_fail) {
             fail_at = t;
@@ -230,8 +236,8 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
         const uint32_t tn = t + 2;
         if (tn < t_end) {
             if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const Stage ns = issue_tile(tn, splits, total, nb, Ak, Av, Bk, Bv, skb, svb, &bar[b],
-                                        threadIdx.x == 0);
+            const Stage ns = issue_tile(tn, t_begin, s_split, total, nb, Ak, Av, Bk, Bv, skb, svb,
+                                        &bar[b], threadIdx.x == 0);
             if (b) stg1 = ns; else stg0 = ns;
         }
     }
@@ -278,58 +284,58 @@ __global__ void __launch_bounds__(CMP_THREADS) k_intersect(
     }
 }
 
-static int compare_grid(uint32_t ntiles) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 152;
-    }
-    uint32_t g = ntiles < (uint32_t)sms * 3 ? ntiles : (uint32_t)sms * 3;
-    if (g > CMP_MAX_CTAS) g = CMP_MAX_CTAS;
-    return g ? (int)g : 1;
+static const size_t kCmpSmem = sizeof(uint32_t) * CMP_BUF * 4;
+
+// Poll limit of each CTA's first wait (a test hook: 0 makes every CTA give up
+// at once, after its copies were issued, so the timeout path can be exercised
+// without a fault).
+static std::atomic<uint32_t> g_first_wait_limit{1u << 22};
+
+void compare_set_first_wait_limit(uint32_t limit) {
+    g_first_wait_limit.store(limit == 0xffffffffu ? (1u << 22) : limit);
 }
 
-static const size_t kCmpSmem = sizeof(uint32_t) * CMP_BUF * 4;
+// The kernel's dynamic shared memory limit, set once per context.
+static cudaError_t compare_attributes() {
+    static PerContext<int> done;
+    int v = 0;
+    return done.get(&v, [](int *out) -> cudaError_t {
+        PHYLO_CHECK(cudaFuncSetAttribute(k_compare, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kCmpSmem));
+        *out = 1;
+        return cudaSuccess;
+    });
+}
 
 cudaError_t compare_launch(cudaStream_t stream, void *scratch, size_t scratch_size,
                            const uint32_t *lk, const float *lv, uint32_t nl, const uint32_t *rk,
                            const float *rv, uint32_t nr, double *d_out, uint32_t **status_out) {
     const uint64_t total = (uint64_t)nl + nr;
     const uint32_t ntiles = (uint32_t)div_up(total, CMP_TILE);
-    Scratch sc(scratch, scratch_size);
-    uint32_t *splits = sc.take<uint32_t>((uint64_t)ntiles + 1 + 1);
-    CmpState *st = sc.take<CmpState>(1);
-    if (!splits || !st) {
+    if (scratch_size < cmp_state_bytes(total) || scratch == nullptr) {
         fprintf(stderr,
                 "phylogenetics: scratch of %zu bytes too small to compare vectors of sizes %u and "
                 "%u\n",
                 scratch_size, nl, nr);
         return cudaErrorInvalidValue;
     }
+    CmpState *st = (CmpState *)scratch;
     if (status_out) *status_out = &st->status;
-    {
-        static uint64_t attr_done = 0;  // one bit per device
-        int dev = 0;
-        PHYLO_CHECK(cudaGetDevice(&dev));
-        if (dev < 64 && !(attr_done >> dev & 1)) {
-            PHYLO_CHECK(cudaFuncSetAttribute(
-                k_intersect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCmpSmem));
-            attr_done |= 1ull << dev;
-        }
-    }
-    const int warps_per_cta = 8;
-    const uint32_t pgrid = (ntiles + 1 + warps_per_cta - 1) / warps_per_cta;
-    k_partition<<<pgrid, warps_per_cta * 32, 0, stream>>>(lk, nl, rk, nr, ntiles, splits, st);
+    PHYLO_CHECK(cudaMemsetAsync(st, 0, 16, stream));  // ticket and status
     if (ntiles == 0) {
         // empty: C = 0
         PHYLO_CHECK(cudaMemsetAsync(d_out, 0, sizeof(double), stream));
-        return cudaGetLastError();
+        return cudaSuccess;
     }
-    const int grid = compare_grid(ntiles);
-    k_intersect<<<grid, CMP_THREADS, kCmpSmem, stream>>>(lk, lv, nl, rk, rv, nr, splits, ntiles,
-                                                        st, d_out);
+    PHYLO_CHECK(compare_attributes());
+    // about three CTAs per SM, at most CMP_MAX_RUN tiles each
+    const uint32_t sms = (uint32_t)device_sm_count();
+    uint32_t grid = min(ntiles, min(3u * sms, CMP_MIN_CAP));
+    uint32_t per = (uint32_t)div_up(ntiles, grid);
+    if (per > CMP_MAX_RUN) per = CMP_MAX_RUN;
+    grid = (uint32_t)div_up(ntiles, per);
+    k_compare<<<grid, CMP_THREADS, kCmpSmem, stream>>>(lk, lv, nl, rk, rv, nr, ntiles, per,
+                                                       g_first_wait_limit.load(), st, d_out);
     return cudaGetLastError();
 }
 
@@ -355,10 +361,10 @@ cudaError_t compare_launch(cudaStream_t stream, void *scratch, size_t scratch_si
 // ---------------------------------------------------------------------------
 
 constexpr uint64_t kStaticCompareMaxEntries = 1ull << 26;
-constexpr size_t kStaticCompareBytes =
-    (((kStaticCompareMaxEntries + CMP_TILE - 1) / CMP_TILE + 2) * sizeof(uint32_t) + 255) / 256 *
-        256 +
-    (sizeof(CmpState) + 255) / 256 * 256;
+constexpr size_t kStaticCompareBytes = cmp_state_bytes(kStaticCompareMaxEntries);
+static_assert(kStaticCompareBytes >= cmp_state_bytes(kStaticCompareMaxEntries) &&
+                  cmp_partials((kStaticCompareMaxEntries + CMP_TILE - 1) / CMP_TILE) >= CMP_MIN_CAP,
+              "the built-in scratch holds the state compare_launch carves at its maximum size");
 
 static __device__ __align__(256) unsigned char g_static_compare_scratch[kStaticCompareBytes];
 
@@ -366,15 +372,11 @@ uint64_t compare_static_max_entries() { return kStaticCompareMaxEntries; }
 size_t compare_static_bytes() { return kStaticCompareBytes; }
 
 // The host name of the array is only a stand-in; the device address comes from
-// cudaGetSymbolAddress, looked up once per device with that device current.
+// cudaGetSymbolAddress, looked up once per context (a device symbol has its own
+// address in every context that loads the module) with that context current.
 static cudaError_t static_scratch_address(void **ptr) {
-    static std::mutex mu;
-    static void *addr[64] = {nullptr};
-    int dev = 0;
-    PHYLO_CHECK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
+    static PerContext<void *> addr;
+    return addr.get(ptr, [](void **out) -> cudaError_t {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_compare_scratch);
         if (e != cudaSuccess) {
@@ -382,10 +384,9 @@ static cudaError_t static_scratch_address(void **ptr) {
                     cudaGetErrorString(e));
             return e;
         }
-        addr[dev] = p;
-    }
-    *ptr = addr[dev];
-    return cudaSuccess;
+        *out = p;
+        return cudaSuccess;
+    });
 }
 
 cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const float *lv,
@@ -407,9 +408,12 @@ cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const
 
 // ---------------------------------------------------------------------------
 // Many pairs per launch.  Tiles of all pairs form one index space (pair p owns
-// tiles [tile_off[p], tile_off[p+1])), persistent CTAs walk contiguous runs of
-// it with the same double-buffered bulk copies, every tile leaves one
-// float-float partial, and k_many_reduce sums each pair's tiles in order.
+// tiles [tile_off[p], tile_off[p+1])).  Persistent CTAs take contiguous runs of
+// at most CMP_MAX_RUN tiles; each CTA first resolves, a warp per tile boundary,
+// the boundary's pair, the pair's vectors and the merge-path split, so the
+// double-buffered bulk copies are issued from shared memory alone.  Every tile
+// leaves one float-float partial, and k_many_reduce sums each pair's tiles in
+// order.
 // ---------------------------------------------------------------------------
 
 struct ManyArgs {
@@ -420,18 +424,28 @@ struct ManyArgs {
     uint32_t *ptiles;          // [P] tiles per pair
     uint64_t *tile_off;        // [P+1]
     uint64_t *scan_tmp;
-    uint32_t *splits;          // [T] left split at each tile start
-    FF *tile_part;             // [T]
+    FF *tile_part;             // [max_tiles]
     uint64_t max_tiles;
+    uint32_t per;              // tiles per CTA
     double *out;               // [P]
     uint32_t *status;
 };
 
-__device__ __forceinline__ uint32_t owner_of(const uint64_t *off, uint32_t n, uint64_t t) {
-    uint32_t lo = 0, hi = n;  // largest p with off[p] <= t
+// Largest p with off[p] <= t (off[0] = 0, off nondecreasing), a warp together:
+// each round splits the range into 32 parts with one load per lane.
+__device__ __forceinline__ uint32_t warp_owner_of(const uint64_t *off, uint32_t n, uint64_t t) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t lo = 0, hi = n;  // answer in [lo, hi)
     while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (off[mid] <= t) lo = mid; else hi = mid;
+        const uint32_t span = hi - lo;
+        const uint32_t step = (span + 31) / 32;
+        const uint32_t i = lo + (lane + 1) * step;  // probe off[i]
+        const bool p = i < hi && __ldg(&off[i]) <= t;
+        const uint32_t cnt = __popc(__ballot_sync(0xffffffffu, p));
+        const uint32_t nlo = lo + cnt * step;
+        const uint32_t nhi = lo + (cnt + 1) * step;
+        lo = nlo;
+        hi = nhi < hi ? nhi : hi;
     }
     return lo;
 }
@@ -443,50 +457,26 @@ __global__ void k_many_tiles(ManyArgs a) {
     a.ptiles[p] = (uint32_t)div_up(tot, CMP_TILE);
 }
 
-// one warp per tile start; grid-stride over the tiles
-__global__ void k_many_partition(ManyArgs a) {
-    const uint64_t T = a.tile_off[a.P];
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = T > a.max_tiles ? DEV_CAPACITY : 0u;
-    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
-    for (uint64_t t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); t < T && t < a.max_tiles;
-         t += warps) {
-        const uint32_t p = owner_of(a.tile_off, a.P, t);
-        const uint32_t va = a.pa[p], vb = a.pb[p];
-        const uint32_t na = a.lnnz[va], nb = a.rnnz[vb];
-        const uint64_t d = (t - a.tile_off[p]) * CMP_TILE;
-        const uint32_t i = warp_merge_path(d, a.lkeys + a.loff[va], na, a.rkeys + a.roff[vb], nb);
-        if ((threadIdx.x & 31) == 0) a.splits[t] = i;
-    }
-}
-
-struct ManyTile {
-    uint32_t i0, i1, j0, j1, j1x;
-    uint32_t va, vb;
+// A tile boundary resolved: its pair, that pair's vectors, the merged position
+// of the boundary within the pair and the left split there.
+struct ManyBound {
+    uint64_t lbase, rbase;   // arena offsets of the two vectors
+    uint64_t d;              // merged position of the boundary within its pair
+    uint32_t p, na, nb, i;   // pair (P: past the last tile), sizes, left split
 };
 
-__device__ __forceinline__ ManyTile many_tile(const ManyArgs &a, uint64_t t) {
-    ManyTile m;
-    const uint32_t p = owner_of(a.tile_off, a.P, t);
-    m.va = a.pa[p];
-    m.vb = a.pb[p];
-    const uint32_t na = a.lnnz[m.va], nb = a.rnnz[m.vb];
-    const uint64_t total = (uint64_t)na + nb;
-    const uint64_t lt = t - a.tile_off[p];
-    const uint64_t d0 = lt * CMP_TILE, d1 = min(d0 + CMP_TILE, total);
-    m.i0 = a.splits[t];
-    m.i1 = (t + 1 < a.tile_off[p + 1]) ? a.splits[t + 1] : na;
-    m.j0 = (uint32_t)(d0 - m.i0);
-    m.j1 = (uint32_t)(d1 - m.i1);
-    m.j1x = m.j1 < nb ? m.j1 + 1 : m.j1;
-    return m;
-}
-
-__device__ __forceinline__ Stage many_issue(const ManyArgs &a, uint64_t t, uint32_t *sk, float *sv,
-                                            uint64_t *bar, bool issue) {
-    const ManyTile m = many_tile(a, t);
-    return issue_ranges(a.lkeys + a.loff[m.va], a.lvals + a.loff[m.va], m.i0, m.i1,
-                        a.rkeys + a.roff[m.vb], a.rvals + a.roff[m.vb], m.j0, m.j1, m.j1x, sk, sv,
-                        bar, issue);
+__device__ __forceinline__ Stage many_issue(const ManyArgs &a, const ManyBound *bd, uint32_t rel,
+                                            uint32_t *sk, float *sv, uint64_t *bar, bool issue) {
+    const ManyBound &b0 = bd[rel];
+    const ManyBound &b1 = bd[rel + 1];
+    const bool same = b1.p == b0.p;  // the next boundary lies inside this tile's pair
+    const uint32_t i0 = b0.i;
+    const uint32_t i1 = same ? b1.i : b0.na;
+    const uint64_t d1 = same ? b1.d : (uint64_t)b0.na + b0.nb;
+    const uint32_t j0 = (uint32_t)(b0.d - i0), j1 = (uint32_t)(d1 - i1);
+    const uint32_t j1x = j1 < b0.nb ? j1 + 1 : j1;
+    return issue_ranges(a.lkeys + b0.lbase, a.lvals + b0.lbase, i0, i1, a.rkeys + b0.rbase,
+                        a.rvals + b0.rbase, j0, j1, j1x, sk, sv, bar, issue);
 }
 
 __global__ void __launch_bounds__(CMP_THREADS) k_many_intersect(ManyArgs a) {
@@ -499,12 +489,33 @@ __global__ void __launch_bounds__(CMP_THREADS) k_many_intersect(ManyArgs a) {
     sv[1] = (float *)(sk[1] + CMP_BUF);
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ FF warp_part[CMP_THREADS / 32];
+    __shared__ ManyBound s_bd[CMP_MAX_RUN + 1];
     __shared__ bool s_fail;
     uint64_t T = a.tile_off[a.P];
+    if (blockIdx.x == 0 && threadIdx.x == 0 && T > a.max_tiles)
+        atomicOr(a.status, (uint32_t)DEV_CAPACITY);
     if (T > a.max_tiles) T = a.max_tiles;
-    const uint64_t per = (T + gridDim.x - 1) / gridDim.x;
-    const uint64_t t_begin = (uint64_t)blockIdx.x * per;
-    const uint64_t t_end = min(T, t_begin + per);
+    const uint64_t t_begin = (uint64_t)blockIdx.x * a.per;
+    const uint64_t t_end = min(T, t_begin + a.per);
+    if (t_begin >= t_end) return;  // the same for every thread of the CTA
+    // resolve the run's boundaries t_begin .. t_end, a warp each
+    const uint32_t nbd = (uint32_t)(t_end - t_begin) + 1;
+    const uint32_t warp = threadIdx.x >> 5;
+    for (uint32_t b = warp; b < nbd; b += CMP_THREADS / 32) {
+        const uint64_t t = t_begin + b;
+        ManyBound m = {0, 0, 0, a.P, 0, 0, 0};
+        if (t < T) {
+            m.p = warp_owner_of(a.tile_off, a.P, t);
+            const uint32_t va = a.pa[m.p], vb = a.pb[m.p];
+            m.na = a.lnnz[va];
+            m.nb = a.rnnz[vb];
+            m.lbase = a.loff[va];
+            m.rbase = a.roff[vb];
+            m.d = (t - a.tile_off[m.p]) * CMP_TILE;
+            m.i = warp_merge_path(m.d, a.lkeys + m.lbase, m.na, a.rkeys + m.rbase, m.nb);
+        }
+        if ((threadIdx.x & 31) == 0) s_bd[b] = m;
+    }
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -513,12 +524,13 @@ __global__ void __launch_bounds__(CMP_THREADS) k_many_intersect(ManyArgs a) {
     }
     __syncthreads();
     Stage stg0 = {0, 0, 0, 0, 0, 0, 0}, stg1 = {0, 0, 0, 0, 0, 0, 0};
-    if (t_begin < t_end) stg0 = many_issue(a, t_begin, sk[0], sv[0], &bar[0], threadIdx.x == 0);
-    if (t_begin + 1 < t_end) stg1 = many_issue(a, t_begin + 1, sk[1], sv[1], &bar[1], threadIdx.x == 0);
+    stg0 = many_issue(a, s_bd, 0, sk[0], sv[0], &bar[0], threadIdx.x == 0);
+    if (t_begin + 1 < t_end) stg1 = many_issue(a, s_bd, 1, sk[1], sv[1], &bar[1], threadIdx.x == 0);
     uint64_t fail_at = ~0ull;
     for (uint64_t t = t_begin; t < t_end; t++) {
-        const int b = (int)((t - t_begin) & 1);
-        const uint32_t phase = (uint32_t)(((t - t_begin) >> 1) & 1);
+        const uint32_t rel = (uint32_t)(t - t_begin);
+        const int b = (int)(rel & 1);
+        const uint32_t phase = (rel >> 1) & 1;
         if (!mbar_wait_bounded(&bar[b], phase)) s_fail = true;
         __syncthreads();
         if (s_fail) {
@@ -535,11 +547,10 @@ __global__ void __launch_bounds__(CMP_THREADS) k_many_intersect(ManyArgs a) {
             for (int w = 0; w < CMP_THREADS / 32; w++) r = ff_merge(r, warp_part[w]);
             a.tile_part[t] = r;
         }
-        const uint64_t tn = t + 2;
-        if (tn < t_end) {
+        if (rel + 2 < (uint32_t)(t_end - t_begin)) {
             if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const Stage ns = many_issue(a, tn, b ? sk[1] : sk[0], b ? sv[1] : sv[0], &bar[b],
-                                        threadIdx.x == 0);
+            const Stage ns = many_issue(a, s_bd, rel + 2, b ? sk[1] : sk[0], b ? sv[1] : sv[0],
+                                        &bar[b], threadIdx.x == 0);
             if (b) stg1 = ns; else stg0 = ns;
         }
         __syncthreads();  // warp_part reused next tile
@@ -577,8 +588,20 @@ __global__ void k_many_reduce(ManyArgs a) {
 
 size_t compare_many_scratch_bytes(uint32_t P, uint64_t max_tiles) {
     return scratch_bytes<uint32_t>(P) + scratch_bytes<uint64_t>((uint64_t)P + 1) +
-           scan_temp_bytes((uint64_t)P + 1) + scratch_bytes<uint32_t>(max_tiles) +
-           scratch_bytes<FF>(max_tiles) + scratch_bytes<uint32_t>(4);
+           scan_temp_bytes((uint64_t)P + 1) + scratch_bytes<FF>(max_tiles ? max_tiles : 1) +
+           scratch_bytes<uint32_t>(4);
+}
+
+static cudaError_t many_attributes() {
+    static PerContext<int> done;
+    int v = 0;
+    return done.get(&v, [](int *out) -> cudaError_t {
+        PHYLO_CHECK(cudaFuncSetAttribute(k_many_intersect,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kCmpSmem));
+        *out = 1;
+        return cudaSuccess;
+    });
 }
 
 cudaError_t compare_many_launch(cudaStream_t st, void *scratch, size_t scratch_size,
@@ -596,34 +619,23 @@ cudaError_t compare_many_launch(cudaStream_t st, void *scratch, size_t scratch_s
     a.ptiles = sc.take<uint32_t>(P);
     a.tile_off = sc.take<uint64_t>((uint64_t)P + 1);
     a.scan_tmp = sc.take<uint64_t>(scan_temp_bytes((uint64_t)P + 1) / 8);
-    a.splits = sc.take<uint32_t>(max_tiles);
-    a.tile_part = sc.take<FF>(max_tiles);
+    a.tile_part = sc.take<FF>(max_tiles ? max_tiles : 1);
     a.status = sc.take<uint32_t>(4);
     a.max_tiles = max_tiles;
     a.out = out;
     if (!a.status) return cudaErrorInvalidValue;
     if (status_out) *status_out = a.status;
-    {
-        static uint64_t attr_done = 0;
-        int dev = 0;
-        PHYLO_CHECK(cudaGetDevice(&dev));
-        if (dev < 64 && !(attr_done >> dev & 1)) {
-            PHYLO_CHECK(cudaFuncSetAttribute(
-                k_many_intersect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCmpSmem));
-            attr_done |= 1ull << dev;
-        }
-    }
+    PHYLO_CHECK(many_attributes());
+    PHYLO_CHECK(cudaMemsetAsync(a.status, 0, sizeof(uint32_t), st));
     k_many_tiles<<<(P + 255) / 256, 256, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.ptiles, P, a.tile_off, a.scan_tmp, st));
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 152;
-    }
-    k_many_partition<<<sms * 4, 256, 0, st>>>(a);
-    k_many_intersect<<<sms * 3, CMP_THREADS, kCmpSmem, st>>>(a);
+    const uint64_t sms = (uint64_t)device_sm_count();
+    uint64_t per = div_up(max_tiles ? max_tiles : 1, 3 * sms);
+    if (per > CMP_MAX_RUN) per = CMP_MAX_RUN;
+    if (per < 1) per = 1;
+    a.per = (uint32_t)per;
+    const uint64_t grid = div_up(max_tiles ? max_tiles : 1, per);
+    k_many_intersect<<<(unsigned)grid, CMP_THREADS, kCmpSmem, st>>>(a);
     k_many_reduce<<<(P + 7) / 8, 256, 0, st>>>(a);
     return cudaGetLastError();
 }

@@ -20,6 +20,11 @@ cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const
                                   uint32_t nl, const uint32_t *rk, const float *rv, uint32_t nr,
                                   double *d_out, uint32_t **status_out);
 uint64_t compare_static_max_entries();
+
+// Poll limit of every compare CTA's first mbarrier wait (0xffffffff: the default).
+// A test hook: 0 makes each CTA give up at once after issuing its copies, which
+// exercises the bounded-wait path (status bit, drained copies) without a fault.
+void compare_set_first_wait_limit(uint32_t limit);
 size_t compare_static_bytes();
 
 // Many pairs per launch: C of pair p = (left vector pa[p], right vector pb[p])

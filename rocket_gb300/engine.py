@@ -8,10 +8,14 @@ correlateGPU for every pair; rocket/scheduler/DeviceWorker.java:118-323):
   device arena (keys | values | offsets), vectors padded to 4 entries so the
   pair kernel can read them with 16-byte loads.
 * :class:`PairEngine` compares every pair of an arena (or a rectangle of row
-  and column vectors) with the window-tiled kernel of csrc/allpairs.cu.  The
-  planner sorts vectors by size, cuts the pair matrix into 16 x 64 tiles and
-  the key space into segments, estimates each item's cost and hands items out
-  longest first.
+  and column vectors).  Two algorithms: ``postings`` (csrc/postings.cu, the
+  default) regroups each key window of a block of row vectors and a block of
+  column vectors by key and forms only the products of shared keys, with exact
+  integer sums; ``window`` (csrc/allpairs.cu) densifies 16 row vectors per key
+  window in shared memory and streams column vectors against them.  The planner
+  sorts vectors by size, cuts the pair matrix into tiles and the key space into
+  segments, estimates each item's cost (for postings from the products of the
+  tile's vector sizes) and hands items out longest first.
 
 All device memory is held in torch tensors; every kernel is this project's
 own (libphylogenetics.so).
@@ -348,24 +352,32 @@ def upload_proteomes(data: np.ndarray, device=None, pinned: Optional[torch.Tenso
 class PairPlan:
     rowids: torch.Tensor       # int32 device
     colids: torch.Tensor
-    tiles: torch.Tensor        # int32 device [ntiles, 4]
+    tiles: torch.Tensor        # int32 device [ntiles, 4] (window) or [ntiles, 8] (postings)
     items: torch.Tensor        # int32 device [nitems, 8]
     ntiles: int
     nitems: int
-    S: int
+    S: int                     # segments per tile (window); the largest per-tile count (postings)
     upper: bool
     mirror: bool
     ldc: int
     est: np.ndarray            # estimated cost per item (launch order)
-    est_product: np.ndarray    # nnz-product estimate per item
     pairs: int                 # valid pairs covered
     host_items: np.ndarray = field(default=None)
     diag: bool = False         # the tiles also cover every vector with itself
+    algorithm: str = "window"
+    nparts: int = 0            # partial blocks the items write
+    host_rowids: np.ndarray = field(default=None)
+    host_colids: np.ndarray = field(default=None)
+    host_tiles: np.ndarray = field(default=None)
+    item_tile: np.ndarray = field(default=None)  # tile of each item (launch order)
+    item_share: np.ndarray = field(default=None)  # fraction of its tile's windows per item
 
 
 @dataclass
 class EngineConfig:
-    wshift: int = 11
+    algorithm: str = "window"  # "window" or "postings" (key-major, exact integer sums)
+    wshift: Optional[int] = None  # key window = 2^wshift ranks (default 9 postings, 11 window)
+    block: int = 128         # postings: vectors per side of a work item (128 or 64)
     tile_rows: int = AP_TI   # row vectors per work item (16 or 32)
     tile_cols: int = AP_TJ   # column vectors per work item (128, 64 or 32; 64 with 32 rows)
     fold: int = 28           # products per FP32 accumulator between compensated folds:
@@ -376,6 +388,12 @@ class EngineConfig:
                              # value makes each pair's arithmetic independent of the plan.
     compress: bool = True    # run the pair kernel on dense key ranks (one arena only)
 
+    def __post_init__(self):
+        if self.algorithm not in ("postings", "window"):
+            raise ValueError(f"unknown pair algorithm {self.algorithm!r}")
+        if self.wshift is None:
+            self.wshift = 9 if self.algorithm == "postings" else 11
+
 
 class PairEngine:
     def __init__(self, arena: Arena, config: Optional[EngineConfig] = None):
@@ -384,16 +402,25 @@ class PairEngine:
         self.L = _native.load()
         self.device = arena.keys.device
         ctas = ctypes.c_int(0)
-        if self.L.phyloPairsSmemBytes(self.cfg.wshift, self.cfg.tile_rows, self.cfg.tile_cols) < 0:
-            raise ValueError(f"unsupported pair tile {self.cfg.tile_rows} x {self.cfg.tile_cols} "
-                             "(16 x 256, 16 x 128, 16 x 64, 16 x 32 or 32 x 64)")
-        check(self.L.phyloPairsPrepare(self.cfg.wshift, self.cfg.tile_rows, self.cfg.tile_cols,
-                                       ctypes.byref(ctas)))
+        if self.cfg.algorithm == "postings":
+            if self.L.phyloPostingsCapacity(self.cfg.block, self.cfg.wshift) < 0:
+                raise ValueError(f"unsupported postings block {self.cfg.block} / window shift "
+                                 f"{self.cfg.wshift} (blocks 128 or 64)")
+            check(self.L.phyloPostingsPrepare(self.cfg.block, self.cfg.wshift, ctypes.byref(ctas)))
+        else:
+            if self.L.phyloPairsSmemBytes(self.cfg.wshift, self.cfg.tile_rows,
+                                          self.cfg.tile_cols) < 0:
+                raise ValueError(f"unsupported pair tile {self.cfg.tile_rows} x "
+                                 f"{self.cfg.tile_cols} (16 x 256, 16 x 128, 16 x 64, 16 x 32 "
+                                 "or 32 x 64)")
+            check(self.L.phyloPairsPrepare(self.cfg.wshift, self.cfg.tile_rows,
+                                           self.cfg.tile_cols, ctypes.byref(ctas)))
         self.ctas_per_sm = max(1, ctas.value)
         props = torch.cuda.get_device_properties(self.device)
         self.sms = props.multi_processor_count
         self.grid = self.sms * self.ctas_per_sm
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.part = None
         self.launches = 0
         self.cmp_scratch = None
@@ -469,67 +496,157 @@ class PairEngine:
         S = max(1, math.ceil(target / max(ntiles, 1)))
         return int(max(1, min(S, self.arena.R // self.cfg.min_windows_per_item)))
 
+    def _tiles(self, nrows: int, ncols: int, triangle: bool):
+        """(row0, nrow, col0, ncol, diag) over positions in the sorted row and
+        column lists.  Window tiles of a triangle start at their first row's own
+        vector, so every vector also meets itself (the self products, the diagonal
+        of the reference's matrix, Main.java:196); postings tiles of a triangle are
+        blocks i <= j, and a diagonal block holds each pair and self product once."""
+        tiles = []
+        if self.cfg.algorithm == "postings":
+            B = self.cfg.block
+            for r0 in range(0, nrows, B):
+                for c0 in range(r0 if triangle else 0, ncols, B):
+                    tiles.append((r0, min(B, nrows - r0), c0, min(B, ncols - c0),
+                                  int(triangle and c0 == r0)))
+            return tiles
+        ti, tj = self.cfg.tile_rows, self.cfg.tile_cols
+        for r0 in range(0, nrows, ti):
+            nr = min(ti, nrows - r0)
+            c = r0 if triangle else 0
+            while c < ncols:
+                nc = min(tj, ncols - c)
+                tiles.append((r0, nr, c, nc, 0))
+                c += nc
+        return tiles
+
+    # cost model of the postings kernel per tile (calibrated against the kernel's
+    # per-item clock64 durations): products + entries regrouped + windows visited
+    PB_COST_PRODUCT = 1.0
+    PB_COST_ENTRY = 4.0
+    PB_COST_WINDOW = 3000.0
+
+    def tile_costs(self, rowids, colids, tiles, row_nnz, col_nnz) -> np.ndarray:
+        """Estimated cost of each tile.  Postings: the nnz-product estimate of the
+        shared-key products, sum over the tile's pairs of nnz_i * nnz_j / U (U =
+        the size of the key space the kernel runs on), plus the entries regrouped
+        and the windows visited.  Window kernel: its linear model (16 products per
+        column entry, the row scatter and a cost per window)."""
+        models = self.tile_cost_models(rowids, colids, tiles, row_nnz, col_nnz)
+        return models["nnz_product"] if self.cfg.algorithm == "postings" else models["linear"]
+
+    def tile_cost_models(self, rowids, colids, tiles, row_nnz, col_nnz) -> dict:
+        """Both cost estimates per tile.  ``nnz_product``: the shared-key products a
+        tile forms, sum over its pairs of nnz_i * nnz_j / U (U = the size of the key
+        space the kernel runs on; a diagonal tile counts each pair once and every
+        self product), plus the entries regrouped and the windows visited (the
+        postings kernel's work).  ``linear``: the window kernel's work, 16 (or
+        tile_rows) products per column entry, the row scatter and a cost per
+        window."""
+        a = self.arena
+        R = a.R
+        tl = np.asarray([t[:5] for t in tiles], np.int64).reshape(-1, 5)
+        cr = np.concatenate([[0.0], np.cumsum(row_nnz[rowids].astype(np.float64))])
+        cc = np.concatenate([[0.0], np.cumsum(col_nnz[colids].astype(np.float64))])
+        sr = cr[tl[:, 0] + tl[:, 1]] - cr[tl[:, 0]]
+        sc = cc[tl[:, 2] + tl[:, 3]] - cc[tl[:, 2]]
+        U = float(max(a.rank_limit if a.index_on_ranks else key_limit(a.alphabet, a.k), 1))
+        q = np.concatenate([[0.0], np.cumsum(row_nnz[rowids].astype(np.float64) ** 2)])
+        sq = q[tl[:, 0] + tl[:, 1]] - q[tl[:, 0]]
+        diag = tl[:, 4] == 1
+        prod = np.where(diag, (sr * sr + sq) / (2.0 * U), sr * sc / U)
+        ent = np.where(diag, sr, sr + sc)
+        return {
+            "nnz_product": (self.PB_COST_PRODUCT * prod + self.PB_COST_ENTRY * ent +
+                            self.PB_COST_WINDOW * R),
+            "linear": self.cfg.tile_rows * sc + 2.0 * sr + 64.0 * R,
+        }
+
+    def item_cost_models(self, plan: "PairPlan") -> dict:
+        """Both estimates per item of ``plan`` (launch order): the tile's estimate
+        times the item's share of the tile's windows."""
+        tiles = [tuple(int(x) for x in t[:4]) + ((int(t[6]) if len(t) > 6 else 0),)
+                 for t in plan.host_tiles]
+        m = self.tile_cost_models(plan.host_rowids, plan.host_colids, tiles,
+                                  self.arena.nnz, self.arena.nnz)
+        return {k: v[plan.item_tile] * plan.item_share for k, v in m.items()}
+
     def _finish_plan(self, rowids, colids, tiles, upper, mirror, ldc, pairs,
                      row_nnz=None, col_nnz=None) -> PairPlan:
         a = self.arena
         ntiles = len(tiles)
-        S = self._segments(ntiles)
         R = a.R
         row_nnz = a.nnz if row_nnz is None else row_nnz
         col_nnz = a.nnz if col_nnz is None else col_nnz
-        tl = np.asarray(tiles, np.int64).reshape(-1, 4)
-        e_tile = np.zeros(ntiles)
-        e_prod = np.zeros(ntiles)
-        for t, (r0, nr, c0, nc) in enumerate(tl):
-            rn = row_nnz[rowids[r0:r0 + nr]].astype(np.float64)
-            cn = col_nnz[colids[c0:c0 + nc]].astype(np.float64)
-            # linear model: 16 products per column entry + row scatter/clear
-            # + a fixed cost per window
-            e_tile[t] = self.cfg.tile_rows * cn.sum() + 2.0 * rn.sum() + 64.0 * R
-            # nnz-product estimate: sum over the tile's pairs of sqrt(nnz_i * nnz_j)
-            e_prod[t] = np.sqrt(rn).sum() * np.sqrt(cn).sum()
-        # item t * S + s: tile t over windows [s R / S, (s + 1) R / S)
-        t_of = np.repeat(np.arange(ntiles, dtype=np.int64), S)
-        s_of = np.tile(np.arange(S, dtype=np.int64), ntiles)
-        items = np.empty((ntiles * S, 8), np.int64)
-        items[:, 0:4] = tl[t_of]
-        items[:, 4] = s_of * R // S
-        items[:, 5] = (s_of + 1) * R // S
-        items[:, 6] = np.arange(ntiles * S, dtype=np.int64)
-        items[:, 7] = t_of
-        est = e_tile[t_of] / S
-        estp = e_prod[t_of] / S
+        rowids = np.asarray(rowids, np.int64)
+        colids = np.asarray(colids, np.int64)
+        cost = self.tile_costs(rowids, colids, tiles, row_nnz, col_nnz)
+        tl = np.asarray([t[:5] for t in tiles], np.int64).reshape(-1, 5)
+        if self.cfg.algorithm == "postings":
+            # segments per tile in proportion to its cost, so that items cost about
+            # the same; a tile's windows are split evenly among its segments
+            if self.cfg.segments > 0:
+                S_t = np.full(ntiles, min(self.cfg.segments, max(R, 1)), np.int64)
+            else:
+                target = cost.sum() / max(self.cfg.items_per_cta * self.grid, 1)
+                S_t = np.clip(np.ceil(cost / max(target, 1e-9)), 1, max(R, 1)).astype(np.int64)
+            part0 = np.concatenate([[0], np.cumsum(S_t)])
+            t_of = np.repeat(np.arange(ntiles, dtype=np.int64), S_t)
+            s_of = np.arange(len(t_of), dtype=np.int64) - part0[t_of]
+            items = np.empty((len(t_of), 8), np.int64)
+            items[:, 0:4] = tl[t_of, 0:4]
+            items[:, 4] = s_of * R // S_t[t_of]
+            items[:, 5] = (s_of + 1) * R // S_t[t_of]
+            items[:, 6] = np.arange(len(t_of), dtype=np.int64)
+            items[:, 7] = tl[t_of, 4]
+            est = cost[t_of] / S_t[t_of]
+            host_tiles = np.zeros((ntiles, 8), np.int64)
+            host_tiles[:, 0:4] = tl[:, 0:4]
+            host_tiles[:, 4] = part0[:-1]
+            host_tiles[:, 5] = S_t
+            host_tiles[:, 6] = tl[:, 4]
+            S = int(S_t.max()) if ntiles else 0
+            nparts = int(part0[-1])
+        else:
+            S = self._segments(ntiles)
+            # item t * S + s: tile t over windows [s R / S, (s + 1) R / S)
+            t_of = np.repeat(np.arange(ntiles, dtype=np.int64), S)
+            s_of = np.tile(np.arange(S, dtype=np.int64), ntiles)
+            items = np.empty((ntiles * S, 8), np.int64)
+            items[:, 0:4] = tl[t_of, 0:4]
+            items[:, 4] = s_of * R // S
+            items[:, 5] = (s_of + 1) * R // S
+            items[:, 6] = np.arange(ntiles * S, dtype=np.int64)
+            items[:, 7] = t_of
+            est = cost[t_of] / S
+            host_tiles = tl[:, 0:4].copy()
+            nparts = ntiles * S
+        share = (items[:, 5] - items[:, 4]) / max(R, 1)
         order = np.argsort(-est, kind="stable")
         items = items[order]
         est = est[order]
-        estp = estp[order]
+        item_tile = t_of[order]
+        share = share[order]
         dev = self.device
         return PairPlan(
-            rowids=torch.from_numpy(np.asarray(rowids, np.int64).astype(np.int32)).to(dev),
-            colids=torch.from_numpy(np.asarray(colids, np.int64).astype(np.int32)).to(dev),
-            tiles=torch.from_numpy(np.asarray(tiles, np.int32).reshape(-1, 4)).to(dev),
+            rowids=torch.from_numpy(rowids.astype(np.int32)).to(dev),
+            colids=torch.from_numpy(colids.astype(np.int32)).to(dev),
+            tiles=torch.from_numpy(host_tiles.astype(np.int32)).to(dev),
             items=torch.from_numpy(items.astype(np.int32)).to(dev),
             ntiles=ntiles, nitems=len(items), S=S, upper=upper, mirror=mirror, ldc=ldc,
-            est=est, est_product=estp, pairs=pairs, host_items=items)
+            est=est, pairs=pairs, host_items=items, algorithm=self.cfg.algorithm,
+            nparts=nparts, host_rowids=rowids, host_colids=colids, host_tiles=host_tiles,
+            item_tile=item_tile, item_share=share)
 
     def plan_triangle(self, ids: Optional[Sequence[int]] = None, ldc: Optional[int] = None) -> PairPlan:
-        """All pairs i < j among ``ids`` (default: every vector of the arena)."""
+        """All pairs i < j among ``ids`` (default: every vector of the arena), and
+        every vector with itself."""
         a = self.arena
         ids = np.arange(a.n) if ids is None else np.asarray(ids, np.int64)
         order = np.argsort(-a.nnz[ids], kind="stable")
         perm = ids[order]
         N = len(perm)
-        tiles = []
-        ti, tj = self.cfg.tile_rows, self.cfg.tile_cols
-        # columns from the tile's first row: every vector meets itself too (the self
-        # products, the diagonal of the reference's matrix, Main.java:196)
-        for r0 in range(0, N, ti):
-            nr = min(ti, N - r0)
-            c = r0
-            while c < N:
-                nc = min(tj, N - c)
-                tiles.append((r0, nr, c, nc))
-                c += nc
+        tiles = self._tiles(N, N, True)
         plan = self._finish_plan(perm, perm, tiles, True, True, ldc or a.n, N * (N - 1) // 2)
         plan.diag = True
         return plan
@@ -544,20 +661,18 @@ class PairEngine:
         cols = np.asarray(col_ids, np.int64)
         rows = rows[np.argsort(-a.nnz[rows], kind="stable")]
         cols = cols[np.argsort(-ca.nnz[cols], kind="stable")]
-        tiles = []
-        ti, tj = self.cfg.tile_rows, self.cfg.tile_cols
-        for r0 in range(0, len(rows), ti):
-            nr = min(ti, len(rows) - r0)
-            for c0 in range(0, len(cols), tj):
-                tiles.append((r0, nr, c0, min(tj, len(cols) - c0)))
+        tiles = self._tiles(len(rows), len(cols), False)
         return self._finish_plan(rows, cols, tiles, False, False, ldc, len(rows) * len(cols),
                                  a.nnz, ca.nnz)
 
     # -- execution -------------------------------------------------------------
     def _parts(self, plan: PairPlan) -> torch.Tensor:
-        need = plan.ntiles * plan.S * self.cfg.tile_rows * self.cfg.tile_cols * 2
+        if plan.algorithm == "postings":
+            need = plan.nparts * self.cfg.block * self.cfg.block * 2  # int64 as int32 pairs
+        else:
+            need = plan.ntiles * plan.S * self.cfg.tile_rows * self.cfg.tile_cols * 2
         if self.part is None or self.part.numel() < need:
-            self.part = torch.empty(need, dtype=torch.float32, device=self.device)
+            self.part = torch.empty(max(need, 2), dtype=torch.float32, device=self.device)
         return self.part
 
     def run(self, plan: PairPlan, out: torch.Tensor, stream=None, item_cycles: torch.Tensor = None,
@@ -565,6 +680,9 @@ class PairEngine:
         """Writes C of every planned pair into ``out`` (float64, row-major, ldc).
         ``events`` = (start, end) CUDA events recorded around the pair kernel."""
         a = self.arena
+        if plan.algorithm != self.cfg.algorithm:
+            raise ValueError(f"plan made for the {plan.algorithm} kernel, engine runs "
+                             f"{self.cfg.algorithm}")
         s_obj = stream if stream is not None else torch.cuda.current_stream(self.device)
         st = int(s_obj.cuda_stream)
         part = self._parts(plan)
@@ -576,18 +694,32 @@ class PairEngine:
         if ca is not a and (a.index_on_ranks or ca.index_on_ranks):
             raise ValueError("dense key ranks need rows and columns in the same arena "
                              "(EngineConfig(compress=False) for two arenas)")
-        check(self.L.phyloPairsLaunch(
-            st, _p(a.pair_keys()), _p(a.values), _p(a.vec_off), _p(a.roff), _p(ca.pair_keys()),
-            _p(ca.values), _p(ca.vec_off), _p(ca.roff), a.R, self.cfg.wshift,
-            _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems, _p(self.counter),
-            _p(part), self.cfg.fold, _p(item_cycles) if item_cycles is not None else 0,
-            self.cfg.tile_rows, self.cfg.tile_cols, self.grid))
-        if events is not None:
-            events[1].record(s_obj)
-        check(self.L.phyloPairsReduce(
-            st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, self.cfg.tile_rows, self.cfg.tile_cols,
-            _p(plan.rowids), _p(plan.colids), _p(out), plan.ldc,
-            (2 if plan.diag and diagonal else 1) if plan.upper else 0, int(plan.mirror)))
+        cyc = _p(item_cycles) if item_cycles is not None else 0
+        if plan.algorithm == "postings":
+            check(self.L.phyloPostingsLaunch(
+                st, _p(a.pair_keys()), _p(a.values), _p(a.vec_off), _p(a.roff),
+                _p(ca.pair_keys()), _p(ca.values), _p(ca.vec_off), _p(ca.roff), a.R,
+                self.cfg.wshift, _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems,
+                _p(self.counter), _p(part), _p(self.status), cyc, self.cfg.block, self.grid))
+            if events is not None:
+                events[1].record(s_obj)
+            check(self.L.phyloPostingsReduce(
+                st, _p(part), _p(plan.tiles), plan.ntiles, self.cfg.block, _p(plan.rowids),
+                _p(plan.colids), _p(out), plan.ldc, int(plan.diag and diagonal),
+                int(plan.mirror)))
+        else:
+            check(self.L.phyloPairsLaunch(
+                st, _p(a.pair_keys()), _p(a.values), _p(a.vec_off), _p(a.roff),
+                _p(ca.pair_keys()), _p(ca.values), _p(ca.vec_off), _p(ca.roff), a.R,
+                self.cfg.wshift, _p(plan.rowids), _p(plan.colids), _p(plan.items), plan.nitems,
+                _p(self.counter), _p(part), self.cfg.fold, cyc, self.cfg.tile_rows,
+                self.cfg.tile_cols, self.grid))
+            if events is not None:
+                events[1].record(s_obj)
+            check(self.L.phyloPairsReduce(
+                st, _p(part), _p(plan.tiles), plan.ntiles, plan.S, self.cfg.tile_rows,
+                self.cfg.tile_cols, _p(plan.rowids), _p(plan.colids), _p(out), plan.ldc,
+                (2 if plan.diag and diagonal else 1) if plan.upper else 0, int(plan.mirror)))
         self.launches += 3  # counter fill, pair kernel, reduction
         if diagonal and plan.upper and not plan.diag:
             maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
@@ -599,6 +731,10 @@ class PairEngine:
             self.launches += 2
         self._fix_nonfinite(plan, out, s_obj, col_arena, diag=diagonal and plan.diag)
 
+    def device_status(self) -> int:
+        """DeviceError bits the postings kernel recorded (synchronises); 0 = none."""
+        return int(self.status.item())
+
     def _fix_nonfinite(self, plan: PairPlan, out: torch.Tensor, stream,
                        col_arena: Optional[Arena] = None, diag: bool = False) -> None:
         """Vectors whose values are NaN/inf: recompute their pairs with the
@@ -606,36 +742,34 @@ class PairEngine:
         reference does)."""
         ra = self.arena
         ca = col_arena if col_arena is not None else ra
-        bad_r = set(np.flatnonzero(~np.isfinite(ra.norms[:ra.n])).tolist())
-        bad_c = set(np.flatnonzero(~np.isfinite(ca.norms[:ca.n])).tolist())
-        if not bad_r and not bad_c:
+        bad_r = ~np.isfinite(ra.norms[:ra.n])
+        bad_c = ~np.isfinite(ca.norms[:ca.n])
+        if not bad_r.any() and not bad_c.any():
             return
-        st = _stream_handle(stream)
-        if self.cmp_scratch is None:
-            maxn = int(max(ra.nnz.max(), ca.nnz.max()))
-            n = int(self.L.estimateScratchMemory(ra.alphabet.encode(), 3, maxn))
-            self.cmp_scratch = torch.empty(n, dtype=torch.uint8, device=self.device)
-        rows = plan.rowids.cpu().numpy()
-        cols = plan.colids.cpu().numpy()
+        rows, cols = plan.host_rowids, plan.host_colids
+        pa, pb = [], []
+        for t in plan.host_tiles:
+            r0, nr, c0, nc = (int(x) for x in t[:4])
+            I, J = np.meshgrid(np.arange(r0, r0 + nr), np.arange(c0, c0 + nc), indexing="ij")
+            I, J = I.ravel(), J.ravel()
+            if plan.upper:  # positions: pairs i < j, and i == j when the plan holds the diagonal
+                keep = (I < J) | (diag & (I == J))
+                I, J = I[keep], J[keep]
+            r, c = rows[I], cols[J]
+            sel = bad_r[r] | bad_c[c]
+            pa.append(r[sel])
+            pb.append(c[sel])
+        pa = np.concatenate(pa) if pa else np.zeros(0, np.int64)
+        pb = np.concatenate(pb) if pb else np.zeros(0, np.int64)
+        if len(pa) == 0:
+            return
+        vals = self.compare_pairs_merge(pa, pb, col_arena=col_arena, stream=stream)
         flat = out.view(-1)
-        for ti in range(plan.ntiles):
-            r0, nr, c0, nc = (int(x) for x in plan.tiles[ti].cpu().numpy())
-            for i in range(r0, r0 + nr):
-                for j in range(c0, c0 + nc):
-                    r, c = int(rows[i]), int(cols[j])
-                    if plan.upper and not (i < j or (diag and i == j)):
-                        continue
-                    if r not in bad_r and c not in bad_c:
-                        continue
-                    o = flat[r * plan.ldc + c:]
-                    check(self.L.phyloComparePairAsync(
-                        st, _p(self.cmp_scratch), self.cmp_scratch.numel(),
-                        _p(ra.keys[int(ra.off[r]):]), _p(ra.values[int(ra.off[r]):]),
-                        int(ra.nnz[r]), _p(ca.keys[int(ca.off[c]):]),
-                        _p(ca.values[int(ca.off[c]):]), int(ca.nnz[c]), _p(o)))
-                    if plan.mirror:
-                        flat[c * plan.ldc + r] = flat[r * plan.ldc + c]
-
+        with torch.cuda.stream(stream):
+            idx = torch.from_numpy(pa * plan.ldc + pb).to(self.device)
+            flat.index_copy_(0, idx, vals)
+            if plan.mirror:
+                flat.index_copy_(0, torch.from_numpy(pb * plan.ldc + pa).to(self.device), vals)
 
     # -- merge-path algorithm over explicit pairs -------------------------------
     def _nnz_dev(self, arena: Arena) -> torch.Tensor:
@@ -712,24 +846,28 @@ def tune_key(arena: Arena, n_rows: int, n_cols: int) -> str:
 
 
 TUNE_SPACE = [
-    dict(wshift=11, tile_rows=16, tile_cols=256, fold=28, items_per_cta=8),
-    dict(wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=4),
-    dict(wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=8),
-    dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
-    dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=2),
-    dict(wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=8),
-    dict(wshift=9, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
-    dict(wshift=11, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
-    dict(wshift=9, tile_rows=16, tile_cols=32, fold=28, items_per_cta=4),
-    dict(wshift=10, tile_rows=32, tile_cols=64, fold=28, items_per_cta=4),
+    dict(algorithm="postings", block=128, wshift=9, items_per_cta=4),
+    dict(algorithm="postings", block=128, wshift=9, items_per_cta=8),
+    dict(algorithm="postings", block=128, wshift=8, items_per_cta=4),
+    dict(algorithm="postings", block=128, wshift=10, items_per_cta=4),
+    dict(algorithm="postings", block=64, wshift=9, items_per_cta=4),
+    dict(algorithm="postings", block=64, wshift=10, items_per_cta=4),
+    dict(algorithm="window", wshift=11, tile_rows=16, tile_cols=256, fold=28, items_per_cta=8),
+    dict(algorithm="window", wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=8),
+    dict(algorithm="window", wshift=10, tile_rows=16, tile_cols=64, fold=28, items_per_cta=4),
+    dict(algorithm="window", wshift=10, tile_rows=32, tile_cols=64, fold=28, items_per_cta=4),
 ]
 
 
 def autotune(arena: Arena, ids=None, space=None, repeats: int = 2, use_cache: bool = True,
-             include_merge: bool = True, verbose: bool = False) -> dict:
-    """Times the window kernel under each configuration of ``space`` (and the
-    merge-path kernel) on the all-pair plan of ``ids`` and returns the fastest,
-    caching it per (alphabet, K, size class) in a JSON file."""
+             include_merge: bool = True, verbose: bool = False, prune: float = 0.0) -> dict:
+    """Times the pair kernels under each configuration of ``space`` (postings and
+    window kernels, and optionally the merge-path kernel) on the all-pair plan of
+    ``ids`` and returns the fastest, caching it per (alphabet, K, size class) in a
+    JSON file (the role of phylogenetics/tune.py:25-84 and the tuning entry point
+    native.cu:782-838, over this library's own tunables).  ``prune`` > 0: a
+    candidate whose first (warm) run is slower than prune x the best time so far is
+    recorded with that time and not repeated."""
     import json
     import os
     import time
@@ -753,10 +891,20 @@ def autotune(arena: Arena, ids=None, space=None, repeats: int = 2, use_cache: bo
         saved = arena.index_state()
         eng.ensure_index()
         plan = eng.plan_triangle(ids)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
         eng.run(plan, out, diagonal=False)
+        e1.record()
         torch.cuda.synchronize()
+        first = e0.elapsed_time(e1)
+        so_far = min([r["ms"] for r in results], default=float("inf"))
         best = float("inf")
-        for _ in range(repeats):
+        if prune > 0 and first > prune * so_far:
+            best, repeats_here = first, 0
+        else:
+            repeats_here = repeats
+        for _ in range(repeats_here):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -764,7 +912,7 @@ def autotune(arena: Arena, ids=None, space=None, repeats: int = 2, use_cache: bo
             e1.record()
             torch.cuda.synchronize()
             best = min(best, e0.elapsed_time(e1))
-        results.append(dict(cfg, algorithm="window", ms=best))
+        results.append(dict(cfg, ms=best))
         arena.restore_index(saved)
         if verbose:
             print(results[-1], flush=True)

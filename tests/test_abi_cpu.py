@@ -17,7 +17,7 @@ HEADER = os.path.join(ROOT, "include", "phylogenetics.h")
 def declared_symbols():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return re.findall(r"^\s*(?:long|int)\s+(\w+)\s*\(", text, flags=re.M)
+    return re.findall(r"^\s*(?:long|int|void)\s+(\w+)\s*\(", text, flags=re.M)
 
 
 @pytest.fixture(scope="module")

@@ -45,8 +45,8 @@ def many():
     (10, 16, 32, True), (9, 16, 32, True), (10, 8, 32, False)])
 def test_allpairs_matches_fp64(small, wshift, fold, rows, compress):
     p, arena, C_ref = small
-    eng = PairEngine(arena, EngineConfig(wshift=wshift, fold=fold, tile_rows=rows,
-                                         tile_cols=64 if rows == 32 else 128,
+    eng = PairEngine(arena, EngineConfig(algorithm="window", wshift=wshift, fold=fold,
+                                         tile_rows=rows, tile_cols=64 if rows == 32 else 128,
                                          compress=compress))
     eng.ensure_index()
     plan = eng.plan_triangle()
@@ -62,12 +62,84 @@ def test_allpairs_matches_fp64(small, wshift, fold, rows, compress):
     assert torch.equal(out, out2)
 
 
+@pytest.mark.parametrize("block,wshift,compress", [
+    (128, 9, True), (128, 6, True), (128, 12, True), (64, 9, True), (64, 11, True),
+    (128, 10, False), (64, 12, False)])
+def test_postings_matches_fp64(small, block, wshift, compress):
+    """Key-major engine: products rounded once to 2^-46 and summed exactly, so every
+    C is within (shared keys) * 2^-47 of the FP64 oracle (1e-9 at these sizes);
+    window shift 12 leaves a posting capacity below a window's entries, which
+    exercises the chunked path."""
+    p, arena, C_ref = small
+    eng = PairEngine(arena, EngineConfig(algorithm="postings", block=block, wshift=wshift,
+                                         compress=compress))
+    eng.ensure_index()
+    plan = eng.plan_triangle()
+    out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+    eng.run(plan, out)
+    assert eng.device_status() == 0
+    C = out.cpu().numpy()
+    assert np.abs(C - C_ref).max() <= 1e-9, np.abs(C - C_ref).max()
+    out2 = torch.full_like(out, 3.0)
+    eng.run(plan, out2)
+    assert torch.equal(out, out2)
+
+
+@pytest.mark.parametrize("block,wshift", [(64, 9), (64, 7), (128, 8)])
+def test_postings_many_blocks(many, block, wshift):
+    """90 vectors in blocks of 64: diagonal and off-diagonal tiles, ragged edges; the
+    segment count per tile follows the cost model."""
+    p, arena, C_ref = many
+    eng = PairEngine(arena, EngineConfig(algorithm="postings", block=block, wshift=wshift))
+    eng.ensure_index()
+    plan = eng.plan_triangle()
+    if block == 64:
+        assert plan.ntiles == 3
+    out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+    eng.run(plan, out)
+    assert eng.device_status() == 0
+    assert np.abs(out.cpu().numpy() - C_ref).max() <= 1e-9
+
+
+def test_postings_and_window_agree(many):
+    p, arena, _ = many
+    outs = []
+    for cfg in (EngineConfig(algorithm="postings", block=64, wshift=9),
+                EngineConfig(algorithm="window", wshift=10, tile_rows=16, tile_cols=64)):
+        eng = PairEngine(arena, cfg)
+        eng.ensure_index()
+        out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+        eng.run(eng.plan_triangle(), out)
+        outs.append(out.cpu().numpy())
+    assert np.abs(outs[0] - outs[1]).max() <= 3.6e-6
+
+
+def test_postings_rectangle_two_arenas(small):
+    """Rows and columns from two arenas (raw keys), as the serving path compares a
+    query batch with the resident database."""
+    p, arena, C_ref = small
+    q = synth.workload("uneven1024", n=20, scale=0.05)
+    qa = BatchBuilder("protein", 6).build(torch.from_numpy(q.data[:q.offsets[5]].copy()).cuda(),
+                                           q.offsets[:6])
+    cfg = EngineConfig(algorithm="postings", block=64, wshift=11, compress=False)
+    eq = PairEngine(qa, cfg)
+    eq.ensure_index()
+    ed = PairEngine(arena, cfg)
+    ed.ensure_index()
+    out = torch.zeros((5, arena.n), dtype=torch.float64, device="cuda")
+    plan = eq.plan_rect(np.arange(5), np.arange(arena.n), ldc=arena.n, col_arena=arena)
+    eq.run(plan, out, diagonal=False, col_arena=arena)
+    # the first five proteomes of both workloads are the same sequences
+    assert np.abs(out.cpu().numpy() - C_ref[:5]).max() <= 1e-9
+
+
 @pytest.mark.parametrize("wshift,rows,cols", [(10, 32, 64), (9, 32, 64), (10, 16, 64),
                                               (9, 16, 32), (10, 16, 32), (11, 16, 128),
                                               (10, 16, 128), (11, 16, 256), (9, 16, 256)])
 def test_allpairs_many_tiles(many, wshift, rows, cols):
     p, arena, C_ref = many
-    eng = PairEngine(arena, EngineConfig(wshift=wshift, tile_rows=rows, tile_cols=cols))
+    eng = PairEngine(arena, EngineConfig(algorithm="window", wshift=wshift, tile_rows=rows,
+                                         tile_cols=cols))
     eng.ensure_index()
     plan = eng.plan_triangle()
     assert plan.ntiles > 2
@@ -82,7 +154,8 @@ def test_tile_rows_agree(many):
     p, arena, _ = many
     outs = []
     for rows, cols in ((16, 64), (32, 64), (16, 32), (16, 256)):
-        eng = PairEngine(arena, EngineConfig(wshift=10, tile_rows=rows, tile_cols=cols))
+        eng = PairEngine(arena, EngineConfig(algorithm="window", wshift=10, tile_rows=rows,
+                                             tile_cols=cols))
         eng.ensure_index()
         out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
         eng.run(eng.plan_triangle(), out)
@@ -211,7 +284,7 @@ def test_autotune(small, tmp_path, monkeypatch):
     p, arena, _ = small
     monkeypatch.setenv("ROCKET_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
     r = autotune(arena, repeats=1)
-    assert r["algorithm"] in ("window", "merge") and r["ms"] > 0
+    assert r["algorithm"] in ("postings", "window", "merge") and r["ms"] > 0
     assert len(r["candidates"]) >= 2
     assert autotune(arena)["ms"] == r["ms"]  # served from the cache
 
