@@ -68,9 +68,16 @@ WORKLOAD_TEXTS = {
 
 # DRAM bytes (read + write) and shared-memory wavefronts of one pair-kernel launch,
 # from ncu captures of the same kernel instantiation on the same workload
-# (profiles/ncu_pair_kernel_dram_*.md gives the commands).  Keyed by
+# (profiles/ncu_pair_kernel_counters_fullsize.md gives the commands and figures).  Keyed by
 # (kernel, workload, K, window shift); a launch of anything else reports null.
-PAIR_KERNEL_COUNTERS = {}
+PAIR_KERNEL_COUNTERS = {
+    ("k_allpairs<512,1,2>", "uneven1024", 6, 11): {"dram_bytes": 792_715_175_168,
+                                                   "smem_wavefronts": 153_568_526_951},
+    ("k_allpairs<512,1,4>", "uniform256", 6, 11): {"dram_bytes": 37_824_623_360,
+                                                   "smem_wavefronts": 8_635_090_516},
+    ("k_allpairs<512,1,2>", "sweep512", 7, 11): {"dram_bytes": 62_698_669_056,
+                                                 "smem_wavefronts": 20_748_469_802},
+}
 
 
 def workload_text(name, k, n):
@@ -411,10 +418,9 @@ def run_ours(args):
     arena = builder.build(seq, wl.offsets, stream=stream)
     torch.cuda.synchronize()
     tuned = None
-    if args.algorithm:
-        space = [c for c in BENCH_TUNE_SPACE if c["algorithm"] == args.algorithm]
-    else:
-        space = list(BENCH_TUNE_SPACE)
+    space = [c for c in BENCH_TUNE_SPACE
+             if (not args.algorithm or c["algorithm"] == args.algorithm)
+             and (not args.tile_cols or c.get("tile_cols") == args.tile_cols)]
     fields = {f.name for f in dataclasses.fields(EngineConfig)}
     if not args.no_tune and len(space) > 1:
         t0 = time.perf_counter()
@@ -699,6 +705,8 @@ def main():
                     help="use only the first N proteomes (small profiling cases)")
     ap.add_argument("--algorithm", default=None, choices=["window", "postings"],
                     help="restrict the tuned pair kernel to one algorithm")
+    ap.add_argument("--tile-cols", type=int, default=0, choices=[0, 128, 256],
+                    help="restrict the tuned window kernel to items of this many columns")
     ap.add_argument("--no-tune", action="store_true",
                     help="no tuning: the first configuration of the bench's space")
     ap.add_argument("--no-graph", action="store_true", help="eager launches of the pair phase")
