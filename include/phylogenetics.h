@@ -302,8 +302,12 @@ int phyloKeyRankIndex(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes,
                       long arena_entries, uintptr_t d_union_bits, int window_shift,
                       unsigned int num_windows, uintptr_t d_rank_keys, uintptr_t d_roff);
 
+/* Merged elements per tile of the merge-path kernels. */
+int phyloCompareTileElements(void);
+
 /* Scratch bytes of phyloComparePairsMany for num_pairs pairs and at most
- * max_tiles merge tiles (sum over pairs of ceil((nl + nr) / 4096)). */
+ * max_tiles merge tiles (sum over pairs of ceil((nl + nr) /
+ * phyloCompareTileElements())). */
 long phyloComparePairsManyScratch(int num_pairs, long max_tiles);
 
 /* C of many pairs with the merge-path kernels in one launch sequence: pair p

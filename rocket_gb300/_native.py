@@ -119,6 +119,8 @@ def _declare(L: ctypes.CDLL) -> None:
     L.phyloKeyRankIndex.argtypes = [c_ptr, c_ptr, c_long, c_long, c_ptr, c_ptr, c_int, c_long,
                                     c_long, c_ptr, c_int, c_uint, c_ptr, c_ptr]
     L.phyloKeyRankIndex.restype = c_int
+    L.phyloCompareTileElements.argtypes = []
+    L.phyloCompareTileElements.restype = c_int
     L.phyloComparePairsManyScratch.argtypes = [c_int, c_long]
     L.phyloComparePairsManyScratch.restype = c_long
     L.phyloComparePairsMany.argtypes = [c_ptr, c_ptr, c_long] + [c_ptr] * 10 + [c_int, c_long, c_ptr]
@@ -150,7 +152,7 @@ EXPORTED = [
     "phyloPairsReduce",
     "phyloSelfDot", "phyloSelfDotPartBytes", "phyloKeyRankScratch", "phyloKeyRankBitmapBytes",
     "phyloKeyRanks", "phyloKeyRankIndex",
-    "phyloComparePairsManyScratch",
+    "phyloCompareTileElements", "phyloComparePairsManyScratch",
     "phyloComparePairsMany", "phyloComparePairAsync",
     "phyloPostingsSmemBytes", "phyloPostingsCapacity", "phyloPostingsThreads",
     "phyloPostingsPrepare", "phyloPostingsLaunch", "phyloPostingsReduce",

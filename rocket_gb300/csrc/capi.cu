@@ -232,6 +232,8 @@ int compareCompositionVectorsStatic(uintptr_t stream, uintptr_t d_left_keys_ptr,
     return (int)cudaGetLastError();
 }
 
+int phyloCompareTileElements(void) { return (int)compare_tile_elements(); }
+
 // Test hook of the bounded waits (see include/phylogenetics.h).
 void phyloCompareTestWaitLimit(unsigned int limit) { compare_set_first_wait_limit(limit); }
 
@@ -653,7 +655,7 @@ long phyloSelfDotPartBytes(int num_vectors, long max_vector_len) {
 }
 
 // Scratch bytes of phyloComparePairsMany for P pairs and at most max_tiles
-// merge tiles (sum over pairs of ceil((nl + nr) / 4096)).
+// merge tiles (sum over pairs of ceil((nl + nr) / phyloCompareTileElements())).
 long phyloComparePairsManyScratch(int num_pairs, long max_tiles) {
     return (long)compare_many_scratch_bytes((uint32_t)num_pairs, (uint64_t)max_tiles);
 }

@@ -21,6 +21,9 @@ cudaError_t compare_launch_static(cudaStream_t stream, const uint32_t *lk, const
                                   double *d_out, uint32_t **status_out);
 uint64_t compare_static_max_entries();
 
+// Merged elements per tile of the merge-path kernels (the unit of max_tiles).
+uint32_t compare_tile_elements();
+
 // Poll limit of every compare CTA's first mbarrier wait (0xffffffff: the default).
 // A test hook: 0 makes each CTA give up at once after issuing its copies, which
 // exercises the bounded-wait path (status bit, drained copies) without a fault.

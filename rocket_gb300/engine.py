@@ -793,7 +793,8 @@ class PairEngine:
             out = torch.empty(P, dtype=torch.float64, device=self.device)
         if P == 0:
             return out
-        tiles = int(np.sum((a.nnz[pa] + ca.nnz[pb] + 4095) // 4096))
+        te = int(self.L.phyloCompareTileElements())
+        tiles = int(np.sum((a.nnz[pa] + ca.nnz[pb] + te - 1) // te))
         nbytes = int(self.L.phyloComparePairsManyScratch(P, tiles))
         if getattr(self, "_many_scratch", None) is None or self._many_scratch.numel() < nbytes:
             self._many_scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.device)

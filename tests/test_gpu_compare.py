@@ -50,7 +50,8 @@ def test_bindings_compare_sweep(n, ratio):
 
 
 @pytest.mark.parametrize("nl,nr", [(0, 0), (0, 5), (7, 0), (1, 1), (4096, 0), (2048, 2048),
-                                   (4095, 1), (12288, 4096), (3, 5000), (33333, 1)])
+                                   (4095, 1), (12288, 4096), (3, 5000), (33333, 1),
+                                   (4352, 0), (4351, 1), (8704, 4352), (2176, 2176)])
 def test_edge_sizes(nl, nr):
     rng = np.random.default_rng(nl * 7919 + nr)
     universe = np.sort(rng.choice(10 * (nl + nr) + 10, size=nl + nr + 10, replace=False))
