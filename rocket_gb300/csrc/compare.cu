@@ -8,7 +8,7 @@
 // a contiguous run of tiles:
 //
 //   * one producer warp issues 1-D bulk copies (TMA) of each tile's left and
-//     right key/value ranges into a ring of three shared-memory stages, each
+//     right key/value ranges into a ring of two shared-memory stages, each
 //     completed on an mbarrier; the tiles' splits are known before it starts
 //     (one pair: the CTA's warps find its few boundaries together; many pairs:
 //     a kernel finds every boundary, a thread each);
@@ -43,7 +43,7 @@ constexpr int CMP_THREADS = CMP_CONSUMER_THREADS + 32;    // + one producer warp
 constexpr int CMP_IPT = 17;  // odd: the lanes' merge runs start on different banks
 constexpr int CMP_TILE = CMP_CONSUMER_THREADS * CMP_IPT;  // merged elements per tile
 constexpr int CMP_BUF = CMP_TILE + 20;  // entries per stage per type (A + B + look-ahead)
-constexpr int CMP_STAGES = 3;
+constexpr int CMP_STAGES = 2;  // two stages: three CTAs (24 merging warps) per SM
 constexpr uint32_t CMP_MAX_RUN = 64;    // tiles per CTA at most
 constexpr uint32_t CMP_MIN_CAP = 1024;  // partial slots always carved
 constexpr uint32_t CMP_WAIT = 1u << 22; // default poll limit of a wait
@@ -176,20 +176,32 @@ __device__ __forceinline__ void merge_tile(const Stage &s, const uint32_t *skb, 
         uint32_t mid = (lo + hi) / 2 + 1;
         if (ka[mid - 1] <= kb[d - mid]) lo = mid; else hi = mid - 1;
     }
+    // Past either range a key reads as NOKEY, above every key of a list.  The
+    // left list then always goes first against the right look-ahead element (the
+    // merge path put every remaining left element at or below it), and no step
+    // can find both ranges exhausted (each step consumes one of the thread's
+    // elements).  The next key of each list is loaded before the comparison, so
+    // the loads are off the step-to-step dependency chain.
+    constexpr uint32_t NOKEY = 0xffffffffu;
     uint32_t i = lo, j = d - lo;
     const uint32_t steps = min((uint32_t)CMP_IPT, n - d);
+    uint32_t x = i < s.na ? ka[i] : NOKEY, y = j < s.nbx ? kb[j] : NOKEY;
     for (uint32_t it = 0; it < steps; it++) {
-        const bool has_a = i < s.na, has_b = j < s.nb, has_bx = j < s.nbx;
-        const uint32_t x = has_a ? ka[i] : 0u, y = has_bx ? kb[j] : 0u;
-        const bool take_a = has_a && (!has_b || x <= y);
-        if (take_a && has_bx && x == y) {
+        const uint32_t xn = i + 1 < s.na ? ka[i + 1] : NOKEY;
+        const uint32_t yn = j + 1 < s.nbx ? kb[j + 1] : NOKEY;
+        if (x == y && x != NOKEY) {
             float p, e;
             two_prod(va[i], vb[j], p, e);
             ff_add(acc, p);
             acc.lo = __fadd_rn(acc.lo, e);
         }
-        i += take_a;
-        j += !take_a;
+        if (x <= y) {  // ties go to the left list
+            i++;
+            x = xn;
+        } else {
+            j++;
+            y = yn;
+        }
     }
 }
 
@@ -469,9 +481,9 @@ cudaError_t compare_launch(cudaStream_t stream, void *scratch, size_t scratch_si
         return cudaSuccess;
     }
     PHYLO_CHECK(compare_attributes());
-    // about two CTAs per SM, at most CMP_MAX_RUN tiles each
+    // about three CTAs per SM, at most CMP_MAX_RUN tiles each
     const uint32_t sms = (uint32_t)device_sm_count();
-    uint32_t grid = min(ntiles, min(2u * sms, CMP_MIN_CAP));
+    uint32_t grid = min(ntiles, min(3u * sms, CMP_MIN_CAP));
     uint32_t per = (uint32_t)div_up(ntiles, grid);
     if (per > CMP_MAX_RUN) per = CMP_MAX_RUN;
     grid = (uint32_t)div_up(ntiles, per);
@@ -793,7 +805,7 @@ cudaError_t compare_many_launch(cudaStream_t st, void *scratch, size_t scratch_s
     k_many_owner<<<P, 256, 0, st>>>(a);
     k_many_splits<<<(unsigned)div_up(mt, 256), 256, 0, st>>>(a);
     const uint64_t sms = (uint64_t)device_sm_count();
-    uint64_t per = div_up(mt, 2 * sms);
+    uint64_t per = div_up(mt, 3 * sms);
     if (per > CMP_MAX_RUN) per = CMP_MAX_RUN;
     if (per < 1) per = 1;
     a.per = (uint32_t)per;
