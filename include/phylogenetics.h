@@ -30,7 +30,7 @@ extern "C" {
  * Bytes of device scratch a CompositionVectorKernels instance allocates once
  * and passes to every build and compare call.
  * Replaces: native.cu:705-716 (estimateScratchMemory), bound at
- * Bindings.java:17-20, called at CompositionVectorKernels.java:87.
+ * Bindings.java:17-20, called at CompositionVectorKernels.java:41.
  * Any alphabet other than "DNA" is sized as "protein" (as the reference).
  */
 long estimateScratchMemory(const char *alphabet, int k, int max_vector_size);
@@ -45,7 +45,7 @@ long estimateScratchMemory(const char *alphabet, int k, int max_vector_size);
  * alphabet is neither "DNA" nor "protein".  Synchronous.
  * Replaces: native.cu:718-752 (buildCompositionVector -> build_composition_vector
  * native.cu:258-477), bound at Bindings.java:22-33, called at
- * CompositionVectorKernels.java:91-112.
+ * CompositionVectorKernels.java:45-66.
  */
 int buildCompositionVector(uintptr_t stream, uintptr_t d_temp_storage_ptr, long temp_storage_size,
                            const char *alphabet, int k, uintptr_t d_string_ptr, long string_len,
@@ -59,7 +59,7 @@ int buildCompositionVector(uintptr_t stream, uintptr_t d_temp_storage_ptr, long 
  * declares double (native.cu:755).
  * Replaces: native.cu:755-780 (compareCompositionVectors ->
  * calculate_cosine_similarity native.cu:645-703), bound at Bindings.java:35-45,
- * called at CompositionVectorKernels.java:114-135.
+ * called at CompositionVectorKernels.java:68-89.
  */
 int compareCompositionVectors(uintptr_t stream, uintptr_t d_temp_storage_ptr, long temp_storage_size,
                               uintptr_t d_left_keys_ptr, uintptr_t d_left_values_ptr, int left_size,

@@ -1,10 +1,10 @@
 """Mirror of CompositionVectorKernels (phylogenetics_analysis/kernels/
-CompositionVectorKernels.java:66-135): owns one stream and one scratch buffer
+CompositionVectorKernels.java:32-89): owns one stream and one scratch buffer
 per context and calls the C ABI.  Device memory is held in torch tensors
 (``torch`` is used for allocation and streams only).
 
 The reference class also carries the Java CPU path (buildCPU/compareCPU,
-:137-268); it is not part of the device product and is restated, as a test
+(:91-222); it is not part of the device product and is restated, as a test
 oracle, under ``oracle/``.
 """
 from __future__ import annotations
@@ -26,7 +26,7 @@ def ptr(t: torch.Tensor) -> int:
 class CompositionVectorKernels:
     def __init__(self, alphabet: str, k: int, max_vector_size: int, max_input_size: int = 0,
                  device=None):
-        if k < 3 or k > 25:  # CompositionVectorKernels.java:79
+        if k < 3 or k > 25:  # CompositionVectorKernels.java:33
             raise ValueError(f"k should be in the range 3-25, not {k}")
         self.k = k
         self.alphabet = alphabet
@@ -43,7 +43,7 @@ class CompositionVectorKernels:
 
     def build_vector_gpu(self, d_input: torch.Tensor, d_keys: torch.Tensor,
                          d_values: torch.Tensor, input_len: int = None) -> int:
-        """buildVectorGPU (:91-112): returns the vector size."""
+        """buildVectorGPU (:45-66): returns the vector size."""
         n = d_input.numel() if input_len is None else int(input_len)
         # work queued on other streams that produced the input must be visible
         self.stream.wait_stream(torch.cuda.current_stream(self.device))
@@ -58,7 +58,7 @@ class CompositionVectorKernels:
     def compare_vectors_gpu(self, left_keys: torch.Tensor, left_values: torch.Tensor,
                             left_size: int, right_keys: torch.Tensor, right_values: torch.Tensor,
                             right_size: int, result: torch.Tensor) -> None:
-        """compareVectorsGPU (:114-135): writes C (double) into ``result``."""
+        """compareVectorsGPU (:68-89): writes C (double) into ``result``."""
         self.stream.wait_stream(torch.cuda.current_stream(self.device))
         err = Bindings.INSTANCE.compareCompositionVectors(
             self.stream_handle, ptr(self.scratch), self.scratch.numel(), ptr(left_keys),
