@@ -71,12 +71,12 @@ WORKLOAD_TEXTS = {
 # (profiles/ncu_pair_kernel_counters_fullsize.md gives the commands and figures).  Keyed by
 # (kernel, workload, K, window shift); a launch of anything else reports null.
 PAIR_KERNEL_COUNTERS = {
-    ("k_allpairs<512,1,2>", "uneven1024", 6, 11): {"dram_bytes": 792_715_175_168,
-                                                   "smem_wavefronts": 153_568_526_951},
-    ("k_allpairs<512,1,4>", "uniform256", 6, 11): {"dram_bytes": 37_824_623_360,
-                                                   "smem_wavefronts": 8_635_090_516},
-    ("k_allpairs<512,1,2>", "sweep512", 7, 11): {"dram_bytes": 62_698_669_056,
-                                                 "smem_wavefronts": 20_748_469_802},
+    ("k_allpairs<512,1,2>", "uneven1024", 6, 11): {"dram_bytes": 797_303_764_992,
+                                                   "smem_wavefronts": 132_638_400_837},
+    ("k_allpairs<512,1,2>", "uniform256", 6, 11): {"dram_bytes": 38_922_074_368,
+                                                   "smem_wavefronts": 7_810_176_711},
+    ("k_allpairs<512,1,2>", "sweep512", 7, 11): {"dram_bytes": 63_794_437_376,
+                                                 "smem_wavefronts": 19_710_804_156},
 }
 
 
@@ -421,6 +421,8 @@ def run_ours(args):
     space = [c for c in BENCH_TUNE_SPACE
              if (not args.algorithm or c["algorithm"] == args.algorithm)
              and (not args.tile_cols or c.get("tile_cols") == args.tile_cols)]
+    if args.wshift:
+        space = [dict(c, wshift=args.wshift) if c["algorithm"] == "window" else c for c in space]
     fields = {f.name for f in dataclasses.fields(EngineConfig)}
     if not args.no_tune and len(space) > 1:
         t0 = time.perf_counter()
@@ -707,6 +709,8 @@ def main():
                     help="restrict the tuned pair kernel to one algorithm")
     ap.add_argument("--tile-cols", type=int, default=0, choices=[0, 128, 256],
                     help="restrict the tuned window kernel to items of this many columns")
+    ap.add_argument("--wshift", type=int, default=0,
+                    help="window engine: key window 2^wshift ranks (default: the tuned space's)")
     ap.add_argument("--no-tune", action="store_true",
                     help="no tuning: the first configuration of the bench's space")
     ap.add_argument("--no-graph", action="store_true", help="eager launches of the pair phase")

@@ -9,26 +9,24 @@
 //     roff[v][r] (the multi-way analogue of a merge-path split: the position of
 //     key r*W in every sorted list, found once per vector) gives each vector's
 //     sub-list in every window.
-//   * A work item is 16 row vectors x up to 64 column vectors x a run of
+//   * A work item is 16 row vectors x up to 256 column vectors x a run of
 //     windows.  For each window the 16 row sub-lists are scattered into a
 //     shared-memory table D[key - r*W] of 80-byte records (16 row values +
 //     padding: the odd stride spreads random gathers over the banks; one extra
-//     zero record serves masked lanes).  Four lanes share a column vector and
-//     stream its sub-list in 16-byte groups through a cp.async ring; every entry
-//     (key, b) adds D[key][i] * b to 16 accumulators -- one per row.  Keys
-//     absent from a row read 0, so the column's sum is exactly the
-//     intersection sum.
+//     zero record serves masked lanes).  The item's columns share the CTA's
+//     lanes evenly (two or four lanes per column); a column's lanes stream its
+//     sub-list in 16-byte groups through cp.async rings, and every entry (key, b)
+//     adds D[key][i] * b to 16 accumulators -- one per row.  Keys absent from a
+//     row read 0, so the column's sum is exactly the intersection sum.
 //   * Accumulation: FP32 products summed in FP32 for at most `fold` products,
 //     then folded into a float-float (TwoSum) accumulator.  Bound on the error
 //     of C: (fold + 2) * 2^-24 * sum|a*b| <= (fold + 2) * 2^-24 for unit
 //     vectors (Cauchy-Schwarz).
 //   * Items are handed out by an atomic counter to persistent CTAs in the
 //     order given (the host sorts them by estimated cost, longest first).
-//     Several CTAs share an SM, so one CTA's window barriers overlap another's
-//     work.
-//   * Each item writes a 16 x 64 float-float partial block; ap_reduce sums the
-//     blocks of a tile in a fixed order (double-double), so results do not
-//     depend on scheduling.
+//   * Each item writes a 16 x (item width) float-float partial block;
+//     ap_reduce sums the blocks of a tile in a fixed order (double-double), so
+//     results do not depend on scheduling.
 #include "allpairs.cuh"
 
 namespace phylo {
@@ -81,67 +79,103 @@ __device__ __forceinline__ void fold16(float (&acc)[16], float (&hi)[16], float 
 }
 
 // Per-thread ring of 16-byte column groups (4 keys + 4 values) fetched with
-// cp.async, RING groups ahead of the one being used, so a thread's column stream
-// stays in flight across window barriers.
-#ifndef AP_RING
-#define AP_RING 2
-#endif
-// Row entries per lane prefetched into registers for the next window (at least).
-#ifndef AP_NPF
-#define AP_NPF 4
-#endif
-constexpr int RING = AP_RING;
+// cp.async (L2 only: a column is read once per item, so caching it in L1 would
+// only evict the row side's data), ring_depth(threads) groups ahead of the one
+// being used, so a thread's column stream stays in flight across window barriers.
+// Four groups for the 512-thread kernels (one CTA per SM; the columns of large
+// items stream from DRAM), two for the smaller CTAs, several of which share an SM.
+__host__ __device__ constexpr int ring_depth(int threads) { return threads >= 512 ? 4 : 2; }
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem)
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int RING>
 __device__ __forceinline__ void cp_async_wait_ring() {
     asm volatile("cp.async.wait_group %0;" ::"n"(RING - 1) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-static size_t ap_ring_bytes(int threads) { return (size_t)RING * threads * 32; }
+static size_t ap_ring_bytes(int threads) { return (size_t)ring_depth(threads) * threads * 32; }
 
-__device__ __forceinline__ FF ff_shfl_xor(FF v, int m) {
-    FF r;
-    r.hi = __shfl_xor_sync(0xffffffffu, v.hi, m);
-    r.lo = __shfl_xor_sync(0xffffffffu, v.lo, m);
-    return r;
+// Lanes of an item's columns: column j takes lanes [s_lane0[j], s_lane0[j + 1]),
+// all THREADS lanes split as evenly as possible over the item's columns (at least
+// one each), so the lanes of an item with fewer columns than the tile's width
+// (at the ragged end of a tile row) are not left idle.  (Weighting the split by
+// the columns' entries measured slower on the full uneven1024 workload: the
+// largest tiles' items are bound by the column stream, not by lane work.)
+template <int THREADS>
+__device__ __forceinline__ void assign_lanes(const ApItem &item, uint32_t *s_lane0,
+                                             uint16_t *s_col) {
+    const uint32_t t = threadIdx.x, nc = item.ncol;
+    if (t <= nc && nc > 0) s_lane0[t] = (uint32_t)((uint64_t)t * THREADS / nc);
+    __syncthreads();
+    if (t < nc)
+        for (uint32_t l = s_lane0[t]; l < s_lane0[t + 1]; l++) s_col[l] = (uint16_t)t;
+    __syncthreads();
 }
 
-// Shape of a 16-row work item for a CTA of THREADS threads: LPC lanes per
-// column vector, so THREADS / LPC columns; each warp scatters AP_TI / warps rows,
-// LPR lanes per row.
+// Sums of the lanes of each column, in lane order, into the item's partial block
+// (rows x tj float pairs).  The sums pass through `stage` (8 rows x THREADS float
+// pairs: the idle cp.async ring), eight rows at a time.
+template <int THREADS>
+__device__ __forceinline__ void combine_lanes(const float (&hi)[16], const float (&lo)[16],
+                                              FF *stage, FF *dst, uint32_t tj, bool has_col,
+                                              uint32_t jcol, uint32_t l0, uint32_t q,
+                                              uint32_t lpc) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 8; i++) stage[i * THREADS + threadIdx.x] = FF{hi[8 * h + i], lo[8 * h + i]};
+        __syncthreads();
+        if (has_col) {
+            for (uint32_t i = q; i < 8; i += lpc) {
+                FF v = stage[i * THREADS + l0];
+                for (uint32_t m = 1; m < lpc; m++) v = ff_merge(v, stage[i * THREADS + l0 + m]);
+                dst[(8 * h + i) * tj + jcol] = v;
+            }
+        }
+    }
+}
+
+// Shape of a 16-row work item for a CTA of THREADS threads: THREADS / LPC
+// columns; each warp scatters AP_TI / warps rows, LPR lanes per row, and
+// prefetches NPF entries per lane of each row's next window.  (Scattering rows in
+// 16-byte groups of four entries was measured slower on every workload.)
 template <int THREADS, int LPC>
 struct ApShape {
     static constexpr int NW = THREADS / 32;
     static constexpr int TJ = THREADS / LPC;     // column vectors per item
     static constexpr int RPW = AP_TI / NW;       // rows a warp scatters
     static constexpr int LPR = 32 / RPW;         // lanes per scattered row
-    static constexpr int NPF = RPW < AP_NPF ? AP_NPF : RPW;  // prefetched entries per lane
+    static constexpr int NPF = 4;                // prefetched row entries per lane (>= RPW)
+    static_assert(RPW <= NPF, "rows per warp");
 };
 
-// Column side: LPC lanes (4, or 2 for 256-column items) per column vector.  Lane
-// q of a column streams the column's 4-entry groups q, q+LPC, q+2 LPC, ... through
-// its cp.async ring, so the lanes of a column fetch 16 LPC contiguous bytes per
-// load, and keeps its own 16 accumulators for the whole item; the lanes' sums are
-// combined once, at the end of the item.  Row side: lane (srow, sj) of a warp scatters entries
-// sj, sj + LPR, ... of row warp * RPW + srow; the first NPF * LPR entries of each
-// row's next window are prefetched into registers.
+// Column side: the item's columns share the lanes evenly (assign_lanes), lpc
+// lanes per column.  Lane q of a column streams the column's 4-entry groups q,
+// q + lpc, q + 2 lpc, ... through its cp.async ring, so the lanes of a column fetch
+// 16 lpc contiguous bytes per load, and keeps its own 16 accumulators for the
+// whole item; the lanes' sums are combined once, at the end of the item.  Row
+// side: lane (srow, sj) of a warp scatters entries sj, sj + LPR, ... of row
+// warp * RPW + srow; the first NPF * LPR entries of each row's next window are
+// prefetched into registers.
 template <int THREADS, int MINB, int LPC>
 __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
     using S = ApShape<THREADS, LPC>;
     constexpr int TJ = S::TJ, RPW = S::RPW, LPR = S::LPR, NPF = S::NPF;
+    constexpr int RING = ring_depth(THREADS);
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t W = 1u << a.wshift, wmask = W - 1u;
     float *D = reinterpret_cast<float *>(smem);                    // (W + 1) x 16
     uint4 *ring_k = reinterpret_cast<uint4 *>(smem + (size_t)(W + 1) * D_STRIDE * 4);
     float4 *ring_v = reinterpret_cast<float4 *>(ring_k + RING * THREADS);
     __shared__ uint32_t s_item;
+    __shared__ uint32_t s_lane0[TJ + 1];
+    __shared__ uint16_t s_col[THREADS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t jcol = threadIdx.x / LPC, q = threadIdx.x % LPC;
     const uint32_t srow = lane / LPR, sj = lane % LPR;
     const uint32_t rr = warp * RPW + srow;  // row position this lane scatters
     const int rsrc = (int)(srow * LPR);     // first lane of this row
@@ -159,8 +193,12 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
         const ApItem item = a.items[it];
         const int64_t t_start = clock64();
 
-        // ---- column side
-        const bool has_col = jcol < item.ncol;
+        // ---- column side: lpc lanes of column jcol, this one the q-th
+        assign_lanes<THREADS>(item, s_lane0, s_col);
+        const bool has_col = item.ncol > 0;
+        const uint32_t jcol = has_col ? s_col[threadIdx.x] : 0u;
+        const uint32_t l0 = has_col ? s_lane0[jcol] : threadIdx.x;
+        const uint32_t q = threadIdx.x - l0, lpc = has_col ? s_lane0[jcol + 1] - l0 : 1u;
         const uint32_t cv = has_col ? a.colids[item.col0 + jcol] : 0u;
         const uint64_t cbase = a.col.vec_off[cv];
         const uint32_t *cro = a.col.roff + (uint64_t)cv * Rs;
@@ -177,7 +215,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                 cp_async16(&ring_k[slot_fetch * THREADS + threadIdx.x], a.col.keys + cbase + fetch);
                 cp_async16(&ring_v[slot_fetch * THREADS + threadIdx.x], a.col.vals + cbase + fetch);
             }
-            fetch += 4 * LPC;
+            fetch += 4 * lpc;
             slot_fetch = slot_fetch + 1 == RING ? 0 : slot_fetch + 1;
             cp_async_commit();
         }
@@ -262,7 +300,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
             // this lane's groups of the column that start before c_hi
             if (has_col) {
                 while (cur < c_hi) {
-                    cp_async_wait_ring();
+                    cp_async_wait_ring<RING>();
                     const uint4 kk = ring_k[slot_cur * THREADS + threadIdx.x];
                     const float4 vv = ring_v[slot_cur * THREADS + threadIdx.x];
                     const uint32_t ks[4] = {kk.x, kk.y, kk.z, kk.w};
@@ -285,10 +323,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                         cp_async16(&ring_v[slot_fetch * THREADS + threadIdx.x],
                                    a.col.vals + cbase + fetch);
                     }
-                    fetch += 4 * LPC;
+                    fetch += 4 * lpc;
                     slot_fetch = slot_fetch + 1 == RING ? 0 : slot_fetch + 1;
                     cp_async_commit();
-                    cur += 4 * LPC;
+                    cur += 4 * lpc;
                     slot_cur = slot_cur + 1 == RING ? 0 : slot_cur + 1;
                 }
             }
@@ -308,15 +346,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
         }
         cp_async_wait_all();
         fold16(acc, hi, lo);
-        // combine the column's lanes (fixed order), lane q writes rows q, q+LPC, ...
-        FF *dst = a.part + (uint64_t)item.part * (AP_TI * TJ);
-#pragma unroll
-        for (int i = 0; i < 16; i++) {
-            FF v = {hi[i], lo[i]};
-#pragma unroll
-            for (int m = 1; m < LPC; m <<= 1) v = ff_merge(v, ff_shfl_xor(v, m));
-            if ((uint32_t)(i % LPC) == q) dst[i * TJ + jcol] = v;
-        }
+        combine_lanes<THREADS>(hi, lo, reinterpret_cast<FF *>(ring_k),
+                               a.part + (uint64_t)item.part * (AP_TI * TJ), TJ, has_col, jcol, l0,
+                               q, lpc);
         if (a.item_cycles && threadIdx.x == 0) a.item_cycles[it] = clock64() - t_start;
     }
 }
