@@ -141,7 +141,9 @@ long phyloBuildBatchSummaryBytes(int num_proteomes);
  * rounded up to 4 entries; d_vec_off (uint64[num_proteomes + 1]) receives the
  * offsets; padding entries get key 0xffffffff, value 0.  d_union_bits, when
  * not 0, is a key bitmap (phyloKeyRankBitmapBytes bytes) in which every
- * written key's bit is set, for phyloKeyRanks.  Asynchronous. */
+ * written key's bit is set, for phyloKeyRanks; so are the bits of the few
+ * candidate keys whose alpha is 0, which are not written (the bitmap is marked
+ * per seen (K-1)-mer).  Asynchronous. */
 int phyloBuildBatchEmit(uintptr_t stream, uintptr_t d_scratch, long scratch_size,
                         const char *alphabet, int k, int num_proteomes, long max_candidates,
                         uintptr_t d_keys, uintptr_t d_values, uintptr_t d_vec_off,
@@ -278,9 +280,10 @@ int phyloPostingsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, i
  * num_vectors vectors below d_keys[e] -- a strictly increasing map, so the
  * pair kernel gives the same products on ranks as on keys, over a denser key
  * space; padding keys 0xFFFFFFFF are kept.  key_limit bounds every key (A^K).
- * d_union_bits: the union bitmap of the vectors' keys (bit k of uint32 word
- * k / 32, phyloKeyRankBitmapBytes bytes), as phyloBuildBatchEmit marks it; 0 to
- * build it here.  d_union_size (uint64, device) receives the union size.
+ * d_union_bits: a bitmap holding at least the vectors' keys (bit k of uint32
+ * word k / 32, phyloKeyRankBitmapBytes bytes), as phyloBuildBatchEmit marks it
+ * (ranks then count the marked keys below a key, still strictly increasing over
+ * the vectors' keys); 0 to build the exact union here.  d_union_size (uint64, device) receives the union size.
  * d_rank_keys 0: only the union's prefix is built in the scratch, for
  * phyloKeyRankIndex.  Asynchronous. */
 long phyloKeyRankScratch(long key_limit);

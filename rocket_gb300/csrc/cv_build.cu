@@ -30,6 +30,7 @@
 //   k_norm          per-proteome norm, scale, nnz
 //   (host reads nnz, checks capacity)
 //   k_compact       survivors' keys and normalised values, copied segment by segment
+//   k_union_mark    (with a key bitmap) the candidate keys of every seen (K-1)-mer
 #include "cv_build.cuh"
 #include "rank.cuh"
 #include "scan.cuh"
@@ -400,89 +401,125 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_count(BuildArgs a) {
     }
 }
 
-// Keys staged per warp in shared memory before the coalesced store: 768 for
-// dense bitmaps, 512 for sparse ones (few candidates per warp; a smaller stage
-// keeps more of these latency-bound CTAs resident).
-constexpr uint32_t KEY_STAGE = 768, KEY_STAGE_SPARSE = 512;
-__host__ __device__ inline uint32_t key_stage(uint32_t wpt) {
-    return wpt > 1 ? KEY_STAGE_SPARSE : KEY_STAGE;
+constexpr int MAX_WPT = 8;  // bitmap words per thread of the chunk kernels, at most
+
+__device__ __forceinline__ uint32_t warp_incl_scan_u32(uint32_t v) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= (uint32_t)d) v += o;
+    }
+    return v;
+}
+
+// The lowest lane k whose (non-decreasing) inclusive scan value incl exceeds i;
+// 31 when none does.
+__device__ __forceinline__ uint32_t warp_owner(uint32_t incl, uint32_t i) {
+    uint32_t k = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        const uint32_t v = __shfl_sync(0xffffffffu, incl, (int)(k + step - 1));
+        if (v <= i) k += step;
+    }
+    return k;
 }
 
 // coff[p][q] = candidate offset of seen (K-1)-mer q within proteome p (entries
-// of unseen q are not written); cq = the key q * A + b of every candidate (b
-// over the right-extension mask of q's suffix, ascending), c0a zeroed.  A warp's
-// candidates are the contiguous range of its 32 bitmap words: their keys are
-// assembled in shared memory and stored coalesced (a range larger than the
-// stage is written directly).  grid = (NCH, B)
+// of unseen q are not written); cq = the key q * A + b of every candidate (b over
+// the right-extension mask of q's suffix, ascending), c0a zeroed.  Thread t of
+// the block owns bitmap words [(c * CHUNK_THREADS + t) * wpt, + wpt) and its
+// candidates start at the exclusive scan of the word_cand sums; a warp's 32
+// threads own a contiguous run of words and candidates, which the warp
+// processes together: its seen (K-1)-mers, 32 at a time in order (each lane
+// finds its own by a search over the scan of the words' populations), load
+// their masks together; a warp scan of the mask populations places their
+// candidates, and the keys are written 32 at a time, coalesced -- each lane finds
+// its candidate's (K-1)-mer by a search over that scan and its symbol b by
+// selecting a set bit of the mask.  (One lane per word, each writing its word's
+// 0..32 A candidates, left most lanes idle; a warp per word wasted its scans on
+// the sparse words of K = 7.)
+// grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
-    extern __shared__ uint32_t stage_all[];  // [warps][key_stage(wpt)]
     const int p = blockIdx.y, c = blockIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t kst = key_stage(a.wpt);
-    uint32_t *stage = stage_all + warp * kst;
+    const uint32_t lane = threadIdx.x & 31u;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
     const uint64_t nw = a.T1s / 32;
+    const uint32_t *seen = a.seen1 + (uint64_t)p * nw;
     const uint64_t wd0 = ((uint64_t)c * CHUNK_THREADS + threadIdx.x) * a.wpt;
     uint32_t s = 0;
     for (uint32_t i = 0; i < a.wpt && wd0 + i < nw; i++) s += a.word_cand[(uint64_t)p * nw + wd0 + i];
     uint64_t tot;
     const uint64_t ex = block_excl_scan_u64<CHUNK_THREADS>(s, sw, &tot);
-    uint32_t run =
+    const uint32_t run0 =
         (uint32_t)(a.chunk_cand_off[pc] - a.chunk_cand_off[(uint64_t)p * a.NCH] + ex);
     const uint64_t gb = a.cbase[p];
-    const uint32_t r0 = __shfl_sync(0xffffffffu, run, 0);
-    const uint32_t r1 = __shfl_sync(0xffffffffu, run + s, 31);
-    const uint64_t w0 = gb + r0, w1 = gb + r1;
-    const bool staged = r1 - r0 <= kst;
+    uint32_t run = __shfl_sync(0xffffffffu, run0, 0);
+    const uint32_t r1 = __shfl_sync(0xffffffffu, run0 + s, 31);
     // zero this warp's K-mer count slots (coalesced)
-    for (uint64_t i = w0 + lane; i < w1 && i < a.cand_cap; i += 32) a.c0a[i] = 0u;
-    // this lane's candidates: seen q in ascending order, then b ascending
+    for (uint64_t i = gb + run + lane; i < gb + r1 && i < a.cand_cap; i += 32) a.c0a[i] = 0u;
+    // the warp's words [wbeg, wend), loaded up front (coalesced), lane l holding word
+    // wbeg + 32 t + l of group t; the seen (K-1)-mers of a group are taken 32 at a time
+    const uint64_t wbeg = __shfl_sync(0xffffffffu, wd0, 0);
+    const uint64_t wend = min(wbeg + (uint64_t)32 * a.wpt, nw);
     const uint32_t A = a.A;
-    for (uint32_t wi = 0; wi < a.wpt && wd0 + wi < nw; wi++) {
-        const uint32_t q0 = (uint32_t)((wd0 + wi) * 32);
-        // (every seen (K-1)-mer, also one without candidates: its compact count slot
-        // is zeroed here, and it may be a candidate's suffix)
-        uint32_t rest = a.seen1[(uint64_t)p * nw + wd0 + wi];
-        const uint32_t word = rest;
-        // compact tables: the rank of this word's first seen bit (one load per word)
-        const uint64_t rank0 = a.compact1 ? (uint64_t)a.pw1[(uint64_t)p * nw + wd0 + wi].x : 0;
-        while (rest) {
-            uint32_t qs[4], ms[4];
+    uint32_t wreg[MAX_WPT];
 #pragma unroll
-            for (int t = 0; t < 4; t++) {
-                qs[t] = rest ? q0 + (uint32_t)(__ffs(rest) - 1) : 0xffffffffu;
-                rest &= rest - 1;
-                ms[t] = qs[t] != 0xffffffffu ? ext_mask(a, p, a.fdT2.mod(qs[t])) : 0u;
-            }
-#pragma unroll
-            for (int t = 0; t < 4; t++) {
-                if (qs[t] == 0xffffffffu) break;
-                const uint32_t q = qs[t];
-                const uint64_t qi = a.compact1 ? rank0 + __popc(word & ((1u << (q & 31u)) - 1u))
-                                               : c1_index(a, p, q);
-                if (!a.compact1 || qi < a.cap1) {
-                    a.coff[qi] = run;  // no candidate: its offset is the next one's
-                    if (a.compact1) a.c1[qi] = 0u;  // counted by k_c0_scatter
-                }
-                uint32_t e = ms[t];
-                while (e) {
-                    const uint32_t key = q * A + (uint32_t)(__ffs(e) - 1);
-                    e &= e - 1;
-                    if (staged) {
-                        stage[run - r0] = key;
-                    } else if (gb + run < a.cand_cap) {
-                        a.cq[gb + run] = key;
-                    }
-                    run++;
-                }
-            }
-        }
+    for (int t = 0; t < MAX_WPT; t++) {
+        const uint64_t w = wbeg + 32 * t + lane;
+        wreg[t] = ((uint32_t)t < a.wpt && w < wend) ? seen[w] : 0u;
     }
-    if (staged) {
-        __syncwarp();
-        for (uint32_t i = lane; i < r1 - r0; i += 32)
-            if (w0 + i < a.cand_cap) a.cq[w0 + i] = stage[i];
+#pragma unroll
+    for (int t = 0; t < MAX_WPT; t++) {
+        if ((uint32_t)t >= a.wpt) break;
+        const uint32_t wbits = wreg[t];
+        const uint32_t wincl = warp_incl_scan_u32(__popc(wbits));
+        const uint32_t nseen = __shfl_sync(0xffffffffu, wincl, 31);
+        if (nseen == 0u) continue;
+        const uint64_t wfirst = wbeg + 32 * t;
+        // compact tables: the rank of the group's first seen (K-1)-mer; the i-th seen
+        // (K-1)-mer of the group is then entry P + i
+        const uint64_t P = a.compact1 ? (uint64_t)a.pw1[(uint64_t)p * nw + wfirst].x : 0;
+        for (uint32_t sb = 0; sb < nseen; sb += 32) {
+            const uint32_t i = sb + lane;
+            const uint32_t k = warp_owner(wincl, i);
+            const uint32_t wk = __shfl_sync(0xffffffffu, wbits, (int)k);
+            const uint32_t ik = __shfl_sync(0xffffffffu, wincl, (int)k);
+            const bool ok = i < nseen;
+            uint32_t q = 0, mask = 0;
+            if (ok) {
+                q = (uint32_t)((wfirst + k) * 32) + nth_set_bit(wk, i - (ik - (uint32_t)__popc(wk)));
+                mask = ext_mask(a, p, a.fdT2.mod(q));
+            }
+            const uint32_t n = __popc(mask);
+            const uint32_t cincl = warp_incl_scan_u32(n);
+            const uint32_t ctot = __shfl_sync(0xffffffffu, cincl, 31);
+            // every seen (K-1)-mer, also one without candidates: its offset (the next
+            // candidate's) and, with compact tables, its count slot (counted by
+            // k_c0_scatter)
+            if (ok) {
+                const uint64_t qi = a.compact1 ? P + i : c1_index(a, p, q);
+                if (!a.compact1 || qi < a.cap1) {
+                    a.coff[qi] = run + cincl - n;
+                    if (a.compact1) a.c1[qi] = 0u;
+                }
+            }
+            // their candidate keys, 32 at a time
+            for (uint32_t cb = 0; cb < ctot; cb += 32) {
+                const uint32_t ci = cb + lane;
+                const uint32_t k2 = warp_owner(cincl, ci);
+                const uint32_t m2 = __shfl_sync(0xffffffffu, mask, (int)k2);
+                const uint32_t q2 = __shfl_sync(0xffffffffu, q, (int)k2);
+                const uint32_t i2 = __shfl_sync(0xffffffffu, cincl, (int)k2);
+                if (ci < ctot) {
+                    const uint32_t b = nth_set_bit(m2, ci - (i2 - (uint32_t)__popc(m2)));
+                    const uint64_t dst = gb + run + ci;
+                    if (dst < a.cand_cap) a.cq[dst] = q2 * A + b;
+                }
+            }
+            run += ctot;
+        }
     }
 }
 
@@ -722,17 +759,22 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 6) k_alpha(BuildArgs a) {
 
 // Per proteome: norm = exact sum of the squares rounded once to double
 // (native.cu:415-428 sums the same float squares in double, in CUB's order),
-// scale = sqrt(norm), its reciprocal, nnz, output base.  grid = B, 32 threads.
-__global__ void k_norm(BuildArgs a) {
+// scale = sqrt(norm), its reciprocal, nnz, output base.  grid = B, NORM_THREADS
+// threads (the CTA partials of a proteome summed exactly, in any order).
+constexpr int NORM_THREADS = 256;
+__global__ void __launch_bounds__(NORM_THREADS) k_norm(BuildArgs a) {
+    __shared__ U192 s_acc[NORM_THREADS / 32];
+    __shared__ uint64_t s_m1[NORM_THREADS / 32];
+    __shared__ uint32_t s_bad[NORM_THREADS / 32];
     const int p = blockIdx.x;
-    const int lane = threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t ncta = a.cand_cap / ALPHA_TILE, nseg = a.cand_cap / SEG;
     const uint64_t c0 = min(a.cbase[p] / ALPHA_TILE, ncta);
     const uint64_t c1 = min(a.cbase[p + 1] / ALPHA_TILE, ncta);
     U192 acc = {0, 0, 0};
     uint64_t m1 = 0;
     uint32_t bad = 0;
-    for (uint64_t c = c0 + lane; c < c1; c += 32) {
+    for (uint64_t c = c0 + threadIdx.x; c < c1; c += NORM_THREADS) {
         u192_add(acc, a.cta_norm[3 * c], a.cta_norm[3 * c + 1], a.cta_norm[3 * c + 2]);
         m1 += a.cta_m1[c];
         bad |= a.cta_bad[c];
@@ -745,6 +787,20 @@ __global__ void k_norm(BuildArgs a) {
     }
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (lane == 0) {
+        s_acc[warp] = acc;
+        s_m1[warp] = m1;
+        s_bad[warp] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        acc = s_acc[0];
+        m1 = s_m1[0];
+        bad = s_bad[0];
+        for (int w = 1; w < NORM_THREADS / 32; w++) {
+            u192_add(acc, s_acc[w].w0, s_acc[w].w1, s_acc[w].w2);
+            m1 += s_m1[w];
+            bad |= s_bad[w];
+        }
         // each unit square adds 1.0 = 2^96 units: bit 32 of the middle word
         u192_add(acc, 0, m1 << 32, m1 >> 32);
         double norm = u192_to_double(acc);
@@ -758,6 +814,34 @@ __global__ void k_norm(BuildArgs a) {
         const uint64_t o1 = a.seg_out_off[min(a.cbase[p + 1] / SEG, nseg)];
         a.nnz[p] = o1 - o0;
         a.out_base[p] = o0;
+    }
+}
+
+// Marks in the key bitmap, for every seen (K-1)-mer q of the batch, the keys
+// q * A + b of its candidates (b over the right-extension mask of q's suffix):
+// one or two atomics per seen (K-1)-mer instead of one per written key.  The
+// marked set is a superset of the written keys (a candidate whose alpha is 0 is
+// marked but not written), which is all a key-rank bitmap needs: ranks stay
+// strictly increasing over the written keys.  grid = (NCH, B)
+__global__ void __launch_bounds__(CHUNK_THREADS) k_union_mark(BuildArgs a) {
+    const int p = blockIdx.y, c = blockIdx.x;
+    const uint64_t nw = a.T1s / 32;
+    const uint64_t wd0 = ((uint64_t)c * CHUNK_THREADS + threadIdx.x) * a.wpt;
+    for (uint32_t i = 0; i < a.wpt; i++) {
+        const uint64_t wd = wd0 + i;
+        if (wd >= nw) break;
+        uint32_t bits = a.seen1[(uint64_t)p * nw + wd];
+        while (bits) {
+            const uint32_t q = (uint32_t)(wd * 32) + (uint32_t)(__ffs(bits) - 1);
+            bits &= bits - 1;
+            const uint32_t m = ext_mask(a, p, a.fdT2.mod(q));
+            if (!m) continue;
+            const uint64_t bit = (uint64_t)q * a.A;
+            const uint64_t w = bit >> 5;
+            const uint32_t off = (uint32_t)bit & 31u;
+            atomicOr(&a.union_bits[w], m << off);
+            if (off + a.A > 32u && (m >> (32u - off))) atomicOr(&a.union_bits[w + 1], m >> (32u - off));
+        }
     }
 }
 
@@ -798,7 +882,6 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
         if (dst + i < dst_end) {
             a.out_keys[dst + i] = key;
             a.out_vals[dst + i] = v;
-            if (a.union_bits) atomicOr(&a.union_bits[key >> 5], 1u << (key & 31u));
         }
     }
 }
@@ -819,7 +902,7 @@ int build_geometry(int alpha, int k, BuildGeometry *g) {
     g->T1s = (g->T1 + 31) / 32 * 32;  // whole words of the seen bitmap
     g->T2 = ipow64(A, k - 2);
     g->T2s = (g->T2 + 31) / 32 * 32;
-    g->wpt = g->T1s > (1ull << 24) ? 8 : 1;  // sparse bitmaps: eight words per thread
+    g->wpt = g->T1s > (1ull << 24) ? MAX_WPT : 1;  // sparse bitmaps: eight words per thread
     g->NCH = div_up(g->T1s / 32, (uint64_t)CHUNK_THREADS * g->wpt);
     return 0;
 }
@@ -997,15 +1080,12 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     k_cand_count<<<gch, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.chunk_cand, nc, a.chunk_cand_off, a.scan_tmp, st));
     k_cand_bases<<<1, 32, 0, st>>>(a);
-    const size_t stage_bytes = sizeof(uint32_t) * (CHUNK_THREADS / 32) * key_stage(a.wpt);
-    PHYLO_CHECK(cudaFuncSetAttribute(k_cand_offsets, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)stage_bytes));
-    k_cand_offsets<<<gch, CHUNK_THREADS, stage_bytes, st>>>(a);
+    k_cand_offsets<<<gch, CHUNK_THREADS, 0, st>>>(a);
     k_c0_scatter<<<grid_seq, COUNT_THREADS, 0, st>>>(a);
     const unsigned ncta = (unsigned)(a.cand_cap / ALPHA_TILE);
     k_alpha<<<ncta, CHUNK_THREADS, 0, st>>>(a);
     PHYLO_CHECK(scan_u32_to_u64(a.seg_surv, a.cand_cap / SEG, a.seg_out_off, a.scan_tmp, st));
-    k_norm<<<a.B, 32, 0, st>>>(a);
+    k_norm<<<a.B, NORM_THREADS, 0, st>>>(a);
     k_tuple_value<<<dim3(TUPLE_TABLE / 256, a.B), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
@@ -1013,6 +1093,8 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
 // Phase 2: write survivors to out_keys/out_vals at dst_base[p] (capacity dst_cap[p]).
 cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
     k_compact<<<(unsigned)(a.cand_cap / ALPHA_TILE), CHUNK_THREADS, 0, st>>>(a);
+    if (a.union_bits)
+        k_union_mark<<<dim3((unsigned)a.NCH, (unsigned)a.B), CHUNK_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -1020,7 +1102,8 @@ cudaError_t build_emit(BuildArgs &a, cudaStream_t st) {
 // Kernels one batched Plan + Emit launches: plan k_prep, k_count, k_tables,
 // k_tuple_alpha, k_cand_count, scan (3), k_cand_bases, k_cand_offsets,
 // k_c0_scatter, k_alpha, scan (3), k_norm, k_tuple_value; emit
-// k_arena_offsets, k_compact, k_arena_pad.  (Six memsets are not counted.)
-int build_launches_per_batch() { return 17 + 3; }
+// k_arena_offsets, k_compact, k_union_mark (with a key bitmap), k_arena_pad.  (Six
+// memsets are not counted.)
+int build_launches_per_batch() { return 17 + 4; }
 
 }  // namespace phylo

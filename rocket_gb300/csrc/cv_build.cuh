@@ -108,7 +108,8 @@ struct BuildArgs {
     // output arena
     uint32_t *out_keys;
     float *out_vals;
-    uint32_t *union_bits;     // optional: bit of every written key set (key-rank bitmap)
+    uint32_t *union_bits;     // optional key-rank bitmap: every written key's bit set (and
+                              // those of the few candidates whose alpha is 0)
 };
 
 // Returns 0, -1 (bad alphabet/k) or -2 (keys would not fit uint32).

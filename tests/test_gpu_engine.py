@@ -177,12 +177,30 @@ def test_rectangle_plan(small):
     assert err.max() <= 1e-6
 
 
+def _check_rank_map(arena, keys, rk, union):
+    """rk (the arena's rank keys) is one strictly increasing map of every key:
+    equal keys get equal ranks in every vector, and a larger key a larger rank."""
+    allk = np.concatenate(keys)
+    allr = np.concatenate([rk[int(arena.off[v]):int(arena.off[v]) + int(arena.nnz[v])]
+                           for v in range(arena.n)])
+    order = np.argsort(allk, kind="stable")
+    k_s, r_s = allk[order], allr[order]
+    same = k_s[1:] == k_s[:-1]
+    assert np.all(r_s[1:][same] == r_s[:-1][same])
+    assert np.all(r_s[1:][~same] > r_s[:-1][~same])
+    assert len(union) <= arena.rank_limit and int(r_s[-1]) < arena.rank_limit
+
+
 def test_key_ranks(small):
     p, arena, _ = small
     eng = PairEngine(arena, EngineConfig(wshift=10))
-    eng.ensure_index()
     keys = [arena.host_vector(v)[0] for v in range(arena.n)]
     union = np.unique(np.concatenate(keys))
+    # a bitmap marked from the keys themselves: ranks in the exact union
+    assert arena.union_n == arena.n
+    saved = arena.union_n
+    arena.union_n, arena.ranked = -1, 0
+    eng.ensure_index()
     assert arena.rank_limit == len(union)
     rk = arena.rkeys.cpu().numpy().view(np.uint32)
     for v in range(arena.n):
@@ -195,13 +213,18 @@ def test_key_ranks(small):
         r = np.searchsorted(union, keys[v])
         expect = np.searchsorted(r, np.arange(arena.R + 1, dtype=np.int64) << 10)
         assert np.array_equal(roff[v, :arena.R + 1], expect)
-    # the bitmap the build marked and one marked from the keys give the same ranks
-    assert arena.union_n == arena.n
-    saved = arena.union_n
-    arena.union_n, arena.ranked = -1, 0
+    # the bitmap the build marked (the candidate keys of every seen (K-1)-mer, a
+    # superset of the written keys): one strictly increasing map of the keys, and
+    # the window index over it
+    arena.union_n, arena.ranked = saved, 0
     eng.ensure_index()
-    assert np.array_equal(arena.rkeys.cpu().numpy().view(np.uint32), rk)
-    arena.union_n = saved
+    rk = arena.rkeys.cpu().numpy().view(np.uint32)
+    _check_rank_map(arena, keys, rk, union)
+    roff = arena.roff.cpu().numpy()
+    for v in range(arena.n):
+        o, m = int(arena.off[v]), int(arena.nnz[v])
+        expect = np.searchsorted(rk[o:o + m], np.arange(arena.R + 1, dtype=np.int64) << 10)
+        assert np.array_equal(roff[v, :arena.R + 1], expect)
 
 
 @pytest.mark.parametrize("wshift", [6, 9, 11])
@@ -224,10 +247,14 @@ def test_rank_index_matches_separate_passes(small, wshift):
     roff = torch.full_like(arena.roff, 7)
     assert L.phyloWindowIndex(0, _p(rk), _p(arena.vec_off), n, wshift, R, maxlen, _p(roff)) == 0
     torch.cuda.synchronize()
-    assert int(union.item()) == arena.rank_limit
     used = int(arena.off[n])
-    assert torch.equal(rk[:used], arena.rkeys[:used])
-    assert torch.equal(roff[:n, :R + 1], arena.roff[:n, :R + 1])
+    keys = [arena.host_vector(v)[0] for v in range(n)]
+    exact = np.unique(np.concatenate(keys))
+    assert int(union.item()) == len(exact)
+    rk_h = rk.cpu().numpy().view(np.uint32)
+    for v in range(n):
+        o, m = int(arena.off[v]), int(arena.nnz[v])
+        assert np.array_equal(rk_h[o:o + m], np.searchsorted(exact, keys[v]))
     # both launch shapes: (slice, vector) CTAs (arena size not given) and the walk
     # over the whole arena (chosen for uneven vectors when the size is given)
     entries = int(arena.off[n] - arena.off[0])
