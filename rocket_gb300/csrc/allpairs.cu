@@ -99,6 +99,18 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 static size_t ap_ring_bytes(int threads) { return (size_t)ring_depth(threads) * threads * 32; }
 
+// Entries [e0, e1) of a vector's keys and values (widened to whole 16-byte
+// groups; vectors start on 16-byte boundaries and are padded to whole groups)
+// into L2 with one bulk prefetch each.
+__device__ __forceinline__ void prefetch_l2(const uint32_t *keys, const float *vals, uint32_t e0,
+                                            uint32_t e1) {
+    const uint32_t g0 = e0 & ~3u, g1 = (e1 + 3u) & ~3u;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(keys + g0), "r"(4u * (g1 - g0))
+                 : "memory");
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(vals + g0), "r"(4u * (g1 - g0))
+                 : "memory");
+}
+
 // Lanes of an item's columns: column j takes lanes [s_lane0[j], s_lane0[j + 1]),
 // all THREADS lanes split as evenly as possible over the item's columns (at least
 // one each), so the lanes of an item with fewer columns than the tile's width
@@ -293,6 +305,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_allpairs(ApArgs a) {
                         pv[t] = __ldg(&a.row.vals[rbase + e]);
                     }
                 }
+                // the rest of the row's next window (the scatter loop's loads) into L2,
+                // a whole window's gathers ahead: large rows stream from DRAM
+                if (has_row && sj == 0 && nhi > nlo + NPF * LPR)
+                    prefetch_l2(a.row.keys + rbase, a.row.vals + rbase, nlo + NPF * LPR, nhi);
             }
             const uint32_t c_hi = c_hi_next;
             if (has_col && r + 2 <= a.R) c_hi_next = __ldg(&cro[r + 2]);
