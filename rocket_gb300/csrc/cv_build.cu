@@ -434,14 +434,17 @@ __device__ __forceinline__ uint32_t warp_owner(uint32_t incl, uint32_t i) {
 // processes together: its seen (K-1)-mers, 32 at a time in order (each lane
 // finds its own by a search over the scan of the words' populations), load
 // their masks together; a warp scan of the mask populations places their
-// candidates, and the keys are written 32 at a time, coalesced -- each lane finds
-// its candidate's (K-1)-mer by a search over that scan and its symbol b by
-// selecting a set bit of the mask.  (One lane per word, each writing its word's
+// candidates, each lane writes its candidates into the warp's shared-memory stage
+// at that offset, and the warp stores the stage coalesced.  (One lane per word,
+// each writing its word's
 // 0..32 A candidates, left most lanes idle; a warp per word wasted its scans on
-// the sparse words of K = 7.)
+// the sparse words of K = 7; finding each key's (K-1)-mer by a search over the
+// scan cost about three times the instructions of the stage.)
 // grid = (NCH, B)
 __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
     __shared__ uint64_t sw[CHUNK_THREADS / 32 + 1];
+    __shared__ uint32_t s_stage[CHUNK_THREADS / 32][32 * 21];  // keys of 32 seen (K-1)-mers (A <= 21)
+    uint32_t *stage = s_stage[threadIdx.x >> 5];
     const int p = blockIdx.y, c = blockIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t pc = (uint64_t)p * a.NCH + c;
@@ -505,19 +508,21 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_cand_offsets(BuildArgs a) {
                     if (a.compact1) a.c1[qi] = 0u;
                 }
             }
-            // their candidate keys, 32 at a time
-            for (uint32_t cb = 0; cb < ctot; cb += 32) {
-                const uint32_t ci = cb + lane;
-                const uint32_t k2 = warp_owner(cincl, ci);
-                const uint32_t m2 = __shfl_sync(0xffffffffu, mask, (int)k2);
-                const uint32_t q2 = __shfl_sync(0xffffffffu, q, (int)k2);
-                const uint32_t i2 = __shfl_sync(0xffffffffu, cincl, (int)k2);
-                if (ci < ctot) {
-                    const uint32_t b = nth_set_bit(m2, ci - (i2 - (uint32_t)__popc(m2)));
-                    const uint64_t dst = gb + run + ci;
-                    if (dst < a.cand_cap) a.cq[dst] = q2 * A + b;
+            // their candidate keys: each lane writes its own (at most A) into the warp's
+            // stage at its scanned offset, then the warp stores them coalesced
+            {
+                uint32_t e = mask, o = cincl - n;
+                while (e) {
+                    stage[o++] = q * A + (uint32_t)(__ffs(e) - 1);
+                    e &= e - 1;
                 }
             }
+            __syncwarp();
+            for (uint32_t ci = lane; ci < ctot; ci += 32) {
+                const uint64_t dst = gb + run + ci;
+                if (dst < a.cand_cap) a.cq[dst] = stage[ci];
+            }
+            __syncwarp();
             run += ctot;
         }
     }
