@@ -46,6 +46,19 @@ constexpr int CHUNK_THREADS = 256;
 // helpers
 // ---------------------------------------------------------------------------
 
+// Batch bases (cbase: B + 1 entries) staged in shared memory when they fit, so
+// that finding a CTA's proteome is one round of parallel loads instead of a chain
+// of dependent ones per thread (k_compact; in the kernels whose tables rely on L1
+// the staging measured slower).
+constexpr int SMEM_BASES = 256;
+__device__ __forceinline__ const uint64_t *stage_bases(const uint64_t *__restrict__ g, int n,
+                                                       uint64_t *s) {
+    if (n > SMEM_BASES) return g;
+    for (int i = threadIdx.x; i <= n; i += blockDim.x) s[i] = g[i];
+    __syncthreads();
+    return s;
+}
+
 __device__ __forceinline__ int find_owner(const uint64_t *__restrict__ base, int n, uint64_t t) {
     // largest p with base[p] <= t, base has n+1 entries, base[0] = 0
     int lo = 0, hi = n;
@@ -855,9 +868,11 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_union_mark(BuildArgs a) {
 // its correctly rounded reciprocal and one FMA correction (Markstein), which
 // yields the correctly rounded double quotient.  grid = cand_cap / ALPHA_TILE
 __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
+    __shared__ uint64_t s_base[SMEM_BASES + 1];
     const uint64_t c = blockIdx.x, g0 = c * ALPHA_TILE;
     if (g0 >= min(*a.cand_total, a.cand_cap)) return;
-    const int p = find_owner(a.cbase, a.B, g0);
+    const uint64_t *cb = stage_bases(a.cbase, a.B, s_base);
+    const int p = find_owner(cb, a.B, g0);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t seg = c * (ALPHA_TILE / SEG) + w;
     const uint32_t n = a.seg_surv[seg];
@@ -870,23 +885,35 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
     const float *vtab = a.vtab + (uint64_t)p * TUPLE_TABLE;
     const bool finite = isfinite(scale) && scale > 0.0;
     const float vm1 = __double2float_rn(-rs);  // RN(-1/scale) == -RN(1/scale)
-    for (uint32_t i = lane; i < n; i += 32) {
-        const uint32_t bits = a.c0a[src + i];
-        const uint32_t key = a.cq[src + i];
-        const float f = __uint_as_float(bits);
-        float v;
-        if ((bits & TUPLE_TAG) == TUPLE_TAG) {
-            v = __ldg(&vtab[bits & ~TUPLE_TAG]);
-        } else if (!finite || !isfinite(f)) {
-            v = __double2float_rn(__ddiv_rn((double)f, scale));
-        } else if (f == -1.0f) {
-            v = vm1;
-        } else {
-            v = div_by_scale(f, scale, rs);
+    // four entries per lane in flight: loads first, then the stores
+    constexpr int U = 4;
+    for (uint32_t i0 = 0; i0 < n; i0 += 32 * U) {
+        uint32_t bits[U], key[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint32_t i = i0 + 32 * u + lane;
+            bits[u] = i < n ? a.c0a[src + i] : 0u;
+            key[u] = i < n ? a.cq[src + i] : 0u;
         }
-        if (dst + i < dst_end) {
-            a.out_keys[dst + i] = key;
-            a.out_vals[dst + i] = v;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint32_t i = i0 + 32 * u + lane;
+            if (i >= n) continue;
+            const float f = __uint_as_float(bits[u]);
+            float v;
+            if ((bits[u] & TUPLE_TAG) == TUPLE_TAG) {
+                v = __ldg(&vtab[bits[u] & ~TUPLE_TAG]);
+            } else if (!finite || !isfinite(f)) {
+                v = __double2float_rn(__ddiv_rn((double)f, scale));
+            } else if (f == -1.0f) {
+                v = vm1;
+            } else {
+                v = div_by_scale(f, scale, rs);
+            }
+            if (dst + i < dst_end) {
+                a.out_keys[dst + i] = key[u];
+                a.out_vals[dst + i] = v;
+            }
         }
     }
 }
