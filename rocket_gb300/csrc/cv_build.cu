@@ -32,6 +32,7 @@
 //   k_compact       survivors' keys and normalised values, copied segment by segment
 //   k_union_mark    (with a key bitmap) the candidate keys of every seen (K-1)-mer
 #include "cv_build.cuh"
+#include "hostctx.cuh"
 #include "rank.cuh"
 #include "scan.cuh"
 
@@ -1068,17 +1069,6 @@ cudaError_t build_carve(const BuildGeometry &g, int B, uint64_t cand_cap, void *
     return cudaSuccess;
 }
 
-static int sm_count() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 152;
-    }
-    return n;
-}
-
 // Phase 1: everything up to per-proteome nnz (no host sync inside).
 cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     const uint64_t nc = (uint64_t)a.B * a.NCH;
@@ -1090,7 +1080,7 @@ cudaError_t build_plan(BuildArgs &a, cudaStream_t st) {
     PHYLO_CHECK(cudaMemsetAsync(a.tot, 0, sizeof(uint32_t) * 4 * a.B, st));
     PHYLO_CHECK(cudaMemsetAsync(a.status, 0, sizeof(uint32_t) * 4, st));
     k_prep<<<1, 32, 0, st>>>(a.B, a.seq_off, a.tile_base);
-    const int grid_seq = sm_count() * 8;
+    const int grid_seq = device_sm_count() * 8;
     if (a.compact1) {
         k_count<true><<<grid_seq, COUNT_THREADS, 0, st>>>(a);
         PHYLO_CHECK(bitmap_prefix_pairs(a.seen1, a.T1s / 32 * a.B, a.p1_partials, a.pw1,
