@@ -615,21 +615,24 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
 // Markov alpha of every candidate (alpha bits replace the count, as
 // native.cu:399 does), flat over the batch's candidate index space: CTA c takes
 // candidates [c * ALPHA_TILE, (c + 1) * ALPHA_TILE) of one proteome, warp w the
-// segment of SEG candidates starting at c * ALPHA_TILE + w * SEG.  Survivors
-// (alpha bits != 0) are compacted, in key order, to the start of their segment:
-// c0a holds their alpha bits (or TUPLE_TAG | tuple), cq their keys; seg_surv the
-// count.  Per-CTA norm partials.  grid = cand_cap / ALPHA_TILE
+// segment of SEG candidates starting at c * ALPHA_TILE + w * SEG.  In place: a
+// seen candidate's c0a slot receives its alpha bits (or TUPLE_TAG | tuple), or
+// CAND_DROP when alpha is 0 (not written out); an unseen one keeps count 0 and
+// stands for alpha -1.  seg_surv = survivors per segment.  Per-CTA norm
+// partials.  grid = cand_cap / ALPHA_TILE
 //
 // Most candidates are K-mers that were not seen (count 0): their alpha is -1
 // (native.cu:392 with p = 0) and needs no table loads.  The others are listed
 // per warp in shared memory and computed densely, 32 lanes on 32 of them, so
 // the long path does not run with most lanes idle.
 constexpr int ALPHA_ILP = 1;  // listed candidates per lane in flight together
+// c0a value of a seen candidate whose alpha is 0: not written out.  No tuple tag
+// (tuple indices stay below TUPLE_TABLE) and no alpha (arithmetic NaNs are
+// 0x7fffffff) has these bits.
+constexpr uint32_t CAND_DROP = 0xffffffffu;
 __global__ void __launch_bounds__(CHUNK_THREADS, 6) k_alpha(BuildArgs a) {
     __shared__ U192 s_norm[CHUNK_THREADS / 32];
     __shared__ uint32_t s_m1[CHUNK_THREADS / 32], s_bad[CHUNK_THREADS / 32];
-    __shared__ uint32_t s_key[CHUNK_THREADS / 32][SEG];    // keys by segment index
-    __shared__ uint32_t s_res[CHUNK_THREADS / 32][SEG];    // stored bits by segment index
     __shared__ uint32_t s_lcnt[CHUNK_THREADS / 32][SEG];   // listed candidates: K-mer count,
     __shared__ uint16_t s_lidx[CHUNK_THREADS / 32][SEG];   // index in the segment
     const uint64_t c = blockIdx.x;
@@ -656,25 +659,23 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 6) k_alpha(BuildArgs a) {
     const uint64_t sbase = g0 + (uint64_t)w * SEG;           // this warp's segment
     const uint32_t loc0 = (uint32_t)(sbase - a.cbase[p]);    // proteome-local index of its start
     U192 acc = {0, 0, 0};
-    uint32_t m1 = 0, bad = 0, nsurv = 0;
+    uint32_t m1 = 0, bad = 0, ndrop = 0;
     constexpr int NI = SEG / 32;  // candidates per lane
-    // phase 1: keys and K-mer counts of the whole segment; candidates that need
-    // the long path (a seen K-mer, or a proteome without K-windows) are listed
-    uint32_t kk[NI], fl[NI];
+    // phase 1: K-mer counts of the whole segment; candidates that need the long path
+    // (a seen K-mer, or a proteome without K-windows) are listed
+    uint32_t fl[NI];
 #pragma unroll
     for (int i = 0; i < NI; i++) {
         const bool ok = loc0 + 32 * i + lane < np;
-        const uint64_t u = sbase + 32 * i + lane;
-        kk[i] = ok ? a.cq[u] : 0u;
-        fl[i] = ok ? a.c0a[u] : 0u;
+        fl[i] = ok ? a.c0a[sbase + 32 * i + lane] : 0u;
     }
-    uint32_t nlist = 0, unseen = 0;  // unseen: bit i = candidate 32 i + lane has alpha -1
+    uint32_t nlist = 0, nok = 0;
 #pragma unroll
     for (int i = 0; i < NI; i++) {
         const bool ok = loc0 + 32 * i + lane < np;
-        s_key[w][32 * i + lane] = kk[i];
         const bool need = ok && (fl[i] != 0u || n0 == 0u);
-        if (ok && !need) unseen |= 1u << i;
+        if (ok && !need) m1++;  // an unseen K-mer: alpha -1, square 1
+        nok += ok;
         const unsigned bal = __ballot_sync(0xffffffffu, need);
         if (need) {
             const uint32_t pos = nlist + __popc(bal & ((1u << lane) - 1u));
@@ -691,7 +692,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 6) k_alpha(BuildArgs a) {
         for (int j = 0; j < ALPHA_ILP; j++) {
             const uint32_t t = t0 + 32 * j + lane;
             const bool ok = t < nlist;
-            key[j] = ok ? s_key[w][s_lidx[w][t]] : 0u;
+            key[j] = ok ? a.cq[sbase + s_lidx[w][t]] : 0u;
             full[j] = ok ? s_lcnt[w][t] : 0u;
             const uint32_t q = A == 21u ? key[j] / 21u : key[j] >> 2;  // protein or DNA alphabet
             const uint32_t b = key[j] - q * A;
@@ -719,7 +720,9 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 6) k_alpha(BuildArgs a) {
                 f = markov_alpha_fast(full[j], pre[j], suf[j], mid[j], n0, n1, n2, prob);
                 stored = __float_as_uint(f);
             }
-            s_res[w][s_lidx[w][t]] = stored;
+            // in place: the alpha bits (or tuple tag), or CAND_DROP for alpha 0
+            a.c0a[sbase + s_lidx[w][t]] = stored ? stored : CAND_DROP;
+            ndrop += stored == 0u;
             if (__float_as_uint(f) != 0u) {
                 const float sq = __fmul_rn(f, f);  // float square, as native.cu:421-423
                 if (sq == 1.0f) m1++;
@@ -728,25 +731,8 @@ __global__ void __launch_bounds__(CHUNK_THREADS, 6) k_alpha(BuildArgs a) {
             }
         }
     }
-    __syncwarp();
-    // phase 3: survivors compacted in key order to the segment's start (positions at
-    // or before a lane's own were read in phase 1); an unseen K-mer's square is 1
-    constexpr uint32_t MINUS_ONE = 0xbf800000u;  // bits of -1.0f
-#pragma unroll
-    for (int i = 0; i < NI; i++) {
-        const bool ok = loc0 + 32 * i + lane < np;
-        const bool un = (unseen >> i) & 1u;
-        const uint32_t stored = un ? MINUS_ONE : (ok ? s_res[w][32 * i + lane] : 0u);
-        const bool surv = stored != 0u;
-        const unsigned bal = __ballot_sync(0xffffffffu, surv);
-        if (surv) {
-            const uint64_t pos = sbase + nsurv + __popc(bal & ((1u << lane) - 1u));
-            a.c0a[pos] = stored;
-            a.cq[pos] = s_key[w][32 * i + lane];
-        }
-        m1 += un;
-        nsurv += __popc(bal);
-    }
+    // phase 3: survivors of the segment (k_compact copies them out in place order)
+    const uint32_t nsurv = __reduce_add_sync(0xffffffffu, nok - ndrop);
     if (lane == 0) a.seg_surv[seg] = nsurv;
     // norm partials (integer: exact and order independent)
     m1 = __reduce_add_sync(0xffffffffu, m1);
@@ -864,10 +850,12 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_union_mark(BuildArgs a) {
     }
 }
 
-// Copies every segment's survivors to the output: keys and float(alpha / scale)
-// (native.cu:460-468).  The division by the per-proteome constant scale uses
-// its correctly rounded reciprocal and one FMA correction (Markstein), which
-// yields the correctly rounded double quotient.  grid = cand_cap / ALPHA_TILE
+// Copies every segment's survivors to the output, in key order: keys and
+// float(alpha / scale) (native.cu:460-468).  A candidate with count 0 is an
+// unseen K-mer (alpha -1); one marked CAND_DROP had alpha 0 and is skipped.  The
+// division by the per-proteome constant scale uses its correctly rounded
+// reciprocal and one FMA correction (Markstein), which yields the correctly
+// rounded double quotient.  grid = cand_cap / ALPHA_TILE
 __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
     __shared__ uint64_t s_base[SMEM_BASES + 1];
     const uint64_t c = blockIdx.x, g0 = c * ALPHA_TILE;
@@ -876,9 +864,12 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
     const int p = find_owner(cb, a.B, g0);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t seg = c * (ALPHA_TILE / SEG) + w;
-    const uint32_t n = a.seg_surv[seg];
-    if (n == 0) return;
+    if (a.seg_surv[seg] == 0) return;
     const uint64_t src = seg * SEG;
+    const uint32_t np =
+        (uint32_t)(a.chunk_cand_off[(uint64_t)(p + 1) * a.NCH] - a.chunk_cand_off[(uint64_t)p * a.NCH]);
+    const uint32_t loc0 = (uint32_t)(src - cb[p]);
+    const uint32_t nc = loc0 < np ? min((uint32_t)SEG, np - loc0) : 0u;  // its candidates
     const uint64_t dst = a.dst_base[p] + (a.seg_out_off[seg] - a.out_base[p]);
     const uint64_t dst_end = a.dst_base[p] + a.dst_cap[p];
     const double scale = a.scale[p];
@@ -886,35 +877,40 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_compact(BuildArgs a) {
     const float *vtab = a.vtab + (uint64_t)p * TUPLE_TABLE;
     const bool finite = isfinite(scale) && scale > 0.0;
     const float vm1 = __double2float_rn(-rs);  // RN(-1/scale) == -RN(1/scale)
-    // four entries per lane in flight: loads first, then the stores
+    // four candidates per lane in flight: loads first, then the stores
     constexpr int U = 4;
-    for (uint32_t i0 = 0; i0 < n; i0 += 32 * U) {
+    uint32_t out = 0;  // survivors written so far
+    for (uint32_t i0 = 0; i0 < nc; i0 += 32 * U) {
         uint32_t bits[U], key[U];
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const uint32_t i = i0 + 32 * u + lane;
-            bits[u] = i < n ? a.c0a[src + i] : 0u;
-            key[u] = i < n ? a.cq[src + i] : 0u;
+            bits[u] = i < nc ? a.c0a[src + i] : CAND_DROP;
+            key[u] = i < nc ? a.cq[src + i] : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
-            const uint32_t i = i0 + 32 * u + lane;
-            if (i >= n) continue;
-            const float f = __uint_as_float(bits[u]);
-            float v;
-            if ((bits[u] & TUPLE_TAG) == TUPLE_TAG) {
-                v = __ldg(&vtab[bits[u] & ~TUPLE_TAG]);
-            } else if (!finite || !isfinite(f)) {
-                v = __double2float_rn(__ddiv_rn((double)f, scale));
-            } else if (f == -1.0f) {
-                v = vm1;
-            } else {
-                v = div_by_scale(f, scale, rs);
+            const bool surv = bits[u] != CAND_DROP;
+            const unsigned bal = __ballot_sync(0xffffffffu, surv);
+            if (surv) {
+                float v;
+                if (bits[u] == 0u) {
+                    v = vm1;  // unseen K-mer: alpha -1
+                } else if ((bits[u] & TUPLE_TAG) == TUPLE_TAG) {
+                    v = __ldg(&vtab[bits[u] & ~TUPLE_TAG]);
+                } else {
+                    const float f = __uint_as_float(bits[u]);
+                    if (!finite || !isfinite(f)) v = __double2float_rn(__ddiv_rn((double)f, scale));
+                    else if (f == -1.0f) v = vm1;
+                    else v = div_by_scale(f, scale, rs);
+                }
+                const uint64_t o = dst + out + __popc(bal & ((1u << lane) - 1u));
+                if (o < dst_end) {
+                    a.out_keys[o] = key[u];
+                    a.out_vals[o] = v;
+                }
             }
-            if (dst + i < dst_end) {
-                a.out_keys[dst + i] = key[u];
-                a.out_vals[dst + i] = v;
-            }
+            out += __popc(bal);
         }
     }
 }
