@@ -71,12 +71,12 @@ WORKLOAD_TEXTS = {
 # (profiles/ncu_pair_kernel_counters_fullsize.md gives the commands and figures).  Keyed by
 # (kernel, workload, K, window shift); a launch of anything else reports null.
 PAIR_KERNEL_COUNTERS = {
-    ("k_allpairs<512,1,2>", "uneven1024", 6, 11): {"dram_bytes": 797_303_764_992,
-                                                   "smem_wavefronts": 132_638_400_837},
-    ("k_allpairs<512,1,2>", "uniform256", 6, 11): {"dram_bytes": 38_922_074_368,
-                                                   "smem_wavefronts": 7_810_176_711},
-    ("k_allpairs<512,1,2>", "sweep512", 7, 11): {"dram_bytes": 63_794_437_376,
-                                                 "smem_wavefronts": 19_710_804_156},
+    ("k_allpairs<512,1,2>", "uneven1024", 6, 11): {"dram_bytes": 826_724_824_832,
+                                                   "smem_wavefronts": 132_650_445_958},
+    ("k_allpairs<512,1,2>", "uniform256", 6, 11): {"dram_bytes": 39_084_610_560,
+                                                   "smem_wavefronts": 7_810_281_080},
+    ("k_allpairs<512,1,2>", "sweep512", 7, 11): {"dram_bytes": 63_618_668_800,
+                                                 "smem_wavefronts": 19_710_517_806},
 }
 
 
