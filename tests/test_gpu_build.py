@@ -36,6 +36,66 @@ def test_known_answers(seq, k, expect):
         assert n == expect
 
 
+# Inputs in which a seen K-mer has alpha exactly 0 (p == p0 in the reference's
+# double arithmetic, native.cu:387-394): a homopolymer protein of K residues, whose
+# one K-mer has full, prefix, suffix and middle counts proportional to the window
+# totals, beside a protein whose K-mer survives.  Found by a seeded search over
+# small inputs with the oracle (a seen candidate missing from the output); the
+# rule drops alpha-0 slots (native.cu:402-458), so these vectors hold fewer
+# entries than candidates.
+ZERO_ALPHA_CASES = [
+    ("DNA", 3, b"T\nCGC"), ("DNA", 4, b"TTTT\nCGTG"), ("DNA", 5, b"CACAC\nAAA"),
+    ("DNA", 6, b"CAATAG\nGGGGGG"), ("DNA", 7, b"TTCTCGA\nTTTTTTT"),
+    ("protein", 3, b"AII\nRRR"), ("protein", 4, b"ALCP\nEEEE"), ("protein", 5, b"PPPP\nHHHHHM"),
+    ("protein", 6, b"RRRRRR\nMLVITL"), ("protein", 3, b"RRRRRRRRRYYYYY\nSSSS"),
+]
+
+
+@pytest.mark.parametrize("alphabet,k,seq", ZERO_ALPHA_CASES)
+def test_zero_alpha_dropped(alphabet, k, seq):
+    r = O.cv_native(seq, k, alphabet, with_values=False)
+    assert 0 < len(r["keys"]) < r["candidates"]  # a seen candidate is dropped
+    assert check_against_oracle(seq, k, alphabet) == len(r["keys"])
+
+
+@pytest.mark.parametrize("alphabet,k", [("protein", 6), ("protein", 4), ("protein", 3),
+                                        ("DNA", 5)])
+def test_zero_alpha_batched(alphabet, k):
+    """The same inputs inside a build batch (protein K = 6: compact (K-1)-mer tables),
+    with a homopolymer proteome (no surviving entry at all) and normal proteomes: every
+    vector against the oracle, and every pair and self product through the pair engine."""
+    from rocket_gb300.engine import PairEngine
+    p = synth.workload("uneven1024", n=2, scale=0.02)
+    cases = [s for a, kk, s in ZERO_ALPHA_CASES if a == alphabet and kk == k]
+    if alphabet == "DNA":
+        normal = [O.bindings_input(3, 2000, "DNA"), O.bindings_input(4, 500, "DNA")]
+        homo = b"G" * 40
+    else:
+        normal = [p.get(0), p.get(1)]
+        homo = b"W" * 40
+    seqs = [normal[0]] + cases + [homo, normal[0][:300] + b"K" * 30 + normal[1][:300], normal[1]]
+    off = np.zeros(len(seqs) + 1, np.int64)
+    np.cumsum([len(x) for x in seqs], out=off[1:])
+    data = torch.from_numpy(np.frombuffer(b"".join(seqs), np.uint8).copy()).cuda()
+    arena = BatchBuilder(alphabet, k, max_batch=4).build(data, off)
+    torch.cuda.synchronize()
+    ref = [O.cv_native(x, k, alphabet) for x in seqs]
+    assert len(ref[len(cases) + 1]["keys"]) == 0  # the homopolymer keeps nothing
+    for i, r in enumerate(ref):
+        kk, v = arena.host_vector(i)
+        assert np.array_equal(kk, r["keys"]), i
+        assert ulp_diff(v, r["values"]) <= 1, i
+    eng = PairEngine(arena)
+    eng.ensure_index()
+    out = torch.zeros((arena.n, arena.n), dtype=torch.float64, device="cuda")
+    eng.run(eng.plan_triangle(), out)
+    C = out.cpu().numpy()
+    for i in range(len(seqs)):
+        for j in range(i, len(seqs)):
+            c = O.compare_fp64(ref[i]["keys"], ref[i]["values"], ref[j]["keys"], ref[j]["values"])
+            assert abs(C[i, j] - c) <= 2e-6, (i, j, C[i, j], c)
+
+
 @pytest.mark.parametrize("k", [3, 4, 5, 6, 7])
 def test_bindings_sweep_protein(k):
     # the sweep of BindingsTest.testBuildVectors (n x seeds, :99-112)

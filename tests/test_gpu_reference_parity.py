@@ -136,6 +136,20 @@ def test_build_full_size_proteomes(ref, bufs, k):
         assert_same_vector(r, o)
 
 
+def test_build_zero_alpha_cases(ref, bufs):
+    """Inputs in which a seen K-mer's alpha is exactly 0 (dropped by both), and a
+    homopolymer whose vector is empty: the same sizes, keys and values as the
+    reference build."""
+    from test_gpu_build import ZERO_ALPHA_CASES
+    cases = list(ZERO_ALPHA_CASES) + [("protein", 5, b"Q" * 50), ("DNA", 8, b"C" * 50)]
+    sizes = []
+    for alphabet, k, seq in cases:
+        r, o = build_both(bufs, seq, k, alphabet, 64)
+        assert_same_vector(r, o)
+        sizes.append(r[0])
+    assert sizes[-1] == 0 and sizes[-2] == 0 and min(sizes[:-2]) > 0
+
+
 def compare_both(bufs, lk, lv, rk, rv):
     st = torch.cuda.current_stream().cuda_stream
     n = max(len(lk), len(rk), 1)
