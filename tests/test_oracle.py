@@ -93,6 +93,22 @@ def test_kat_homopolymer_is_empty():
     assert len(r["keys"]) == 0 and r["candidates"] == 1
 
 
+@pytest.mark.parametrize("alphabet,k,seq", [
+    ("DNA", 3, b"T\nCGC"), ("DNA", 5, b"CACAC\nAAA"), ("DNA", 7, b"TTCTCGA\nTTTTTTT"),
+    ("protein", 3, b"AII\nRRR"), ("protein", 5, b"PPPP\nHHHHHM"), ("protein", 6, b"RRRRRR\nMLVITL"),
+    ("protein", 3, b"RRRRRRRRRYYYYY\nSSSS")])
+def test_kat_alpha_zero_is_dropped(alphabet, k, seq):
+    """A seen K-mer whose alpha is exactly 0 (p == p0: a homopolymer protein of K
+    residues beside another protein) is dropped (native.cu:402-458): the vector
+    holds one entry fewer than the candidates, in both formulations of the rule."""
+    a = O.cv_native(seq, k, alphabet, formulation="slots", with_values=False)
+    b = O.cv_native(seq, k, alphabet, with_values=False)
+    assert np.array_equal(a["keys"], b["keys"])
+    assert np.array_equal(a["alpha"].view(np.uint32), b["alpha"].view(np.uint32))
+    assert 0 < len(b["keys"]) == b["candidates"] - 1
+    assert np.all(b["alpha"] != 0)
+
+
 def test_kat_unseen_kmers_minus_one():
     # "ACA\nCC", K=3: n0=1 (ACA), n1=3 (AC, CA, CC), n2=5 (A A C C C -> A2 C3).
     # Candidates ACA ACC CAC CCA CCC; only ACA was seen:
