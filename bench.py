@@ -640,6 +640,7 @@ def serve_run(args, short: bool = False) -> dict:
     srv.load(db, capacity_vectors=len(wl), capacity_entries=capacity_entries)
     torch.cuda.synchronize()
     t_load = time.perf_counter() - t0
+    tuned = srv.tune()  # item width for query batches
     srv.start()
     nxt = n_db
     for w in range(warm):  # warm-up requests (one proteome each), not measured
@@ -681,7 +682,8 @@ def serve_run(args, short: bool = False) -> dict:
         "db_load_s": t_load, "generate_s": t_gen, "data": "synthetic",
         "config": {"workload": SERVE_TEXT.format(db=n_db, nb=nbatches, rate=args.rate,
                                                  budget=args.budget_gb),
-                   "segments": args.segments, "window_shift": 11, "keys": "raw keys"},
+                   "segments": args.segments, "window_shift": 11, "keys": "raw keys",
+                   "tile_cols": srv.cfg.tile_cols, "tuned": tuned},
         "clocks": clocks.summary(),
     }
     if errors:

@@ -180,6 +180,7 @@ class ServingEngine:
         self.completed: List[Request] = []
         self.threads: List[threading.Thread] = []
         self.slots: List[_Slot] = []
+        self.tuned: Optional[dict] = None
 
     # -- database -----------------------------------------------------------
     def load(self, proteomes: Proteomes, capacity_vectors: Optional[int] = None,
@@ -206,6 +207,40 @@ class ServingEngine:
         db.appended = 0
         self.db = db
         return db
+
+    def tune(self, widths=(128, 256), rows: int = 64, repeats: int = 2) -> dict:
+        """Chooses the width of the pair items for query batches: a rectangle of the
+        first ``rows`` database vectors against the whole database (the shape of a
+        full query batch) is timed under each width and the fastest kept (the role of
+        the reference's tuner, phylogenetics/tune.py:25-84, for serving).  The
+        window width stays: the database's window index is built for it."""
+        if self.db is None or self.db.arena.n == 0:
+            raise RuntimeError("load a database first")
+        db = self.db.arena
+        n = db.n
+        row_ids = np.arange(min(rows, n))
+        out = torch.empty((len(row_ids), n), dtype=torch.float64, device=self.device)
+        results = []
+        for w in widths:
+            cfg = dataclasses.replace(self.cfg, tile_cols=int(w))
+            eng = PairEngine(db, cfg)
+            plan = eng.plan_rect(row_ids, np.arange(n), ldc=n, col_arena=db)
+            eng.run(plan, out, diagonal=False, col_arena=db)  # warm-up
+            torch.cuda.synchronize(self.device)
+            best = float("inf")
+            for _ in range(repeats):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                eng.run(plan, out, diagonal=False, col_arena=db)
+                e1.record()
+                torch.cuda.synchronize(self.device)
+                best = min(best, e0.elapsed_time(e1))
+            results.append({"tile_cols": int(w), "ms": best})
+        win = min(results, key=lambda r: r["ms"])
+        self.cfg = dataclasses.replace(self.cfg, tile_cols=win["tile_cols"])
+        self.tuned = dict(win, rows=len(row_ids), db=n, candidates=results)
+        return self.tuned
 
     # -- request flow ----------------------------------------------------------
     def submit(self, req: Request) -> Request:

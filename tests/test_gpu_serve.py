@@ -83,3 +83,25 @@ def test_appended_queries_join_the_database(data):
         v = O.cv_native(queries[1].get(a), 6)
         exact = O.compare_fp64(q0["keys"], q0["values"], v["keys"], v["values"])
         assert abs(r1.result[0, len(db) + a] - exact) / 2 <= 1e-6
+
+
+def test_tuned_width_serves_the_oracle(data):
+    """tune() times query-shaped rectangles under each item width and keeps the
+    fastest; requests served with it match the oracle."""
+    p, db, queries = data
+    srv = ServingEngine("protein", 6, budget_bytes=40e9, slots=2, max_batch=6,
+                        cfg=EngineConfig(segments=4))
+    srv.load(db)
+    t = srv.tune(widths=(128, 256), rows=8)
+    assert t["tile_cols"] in (128, 256) and len(t["candidates"]) == 2
+    assert srv.cfg.tile_cols == t["tile_cols"]
+    srv.start()
+    r = srv.submit(Request(0, queries[3], append=False))
+    assert r.done.wait(300) and r.error is None, r.error
+    srv.stop()
+    dbv = [O.cv_native(db.get(j), 6) for j in range(len(db))]
+    for a in range(len(queries[3])):
+        qa = O.cv_native(queries[3].get(a), 6)
+        for j in range(len(db)):
+            exact = O.compare_fp64(qa["keys"], qa["values"], dbv[j]["keys"], dbv[j]["values"])
+            assert abs(r.result[a, j] - exact) / 2 <= 1e-6
