@@ -23,13 +23,14 @@
 //                   cbase[p], a multiple of ALPHA_TILE
 //   k_cand_offsets  per-(K-1)-mer candidate offsets; the key of every candidate
 //   k_c0_scatter    K-mer counts into candidate slots (zeroed by k_cand_offsets)
-//   k_alpha         Markov alpha (reference double order) of every candidate, flat
-//                   over the candidates; each warp compacts its segment's survivors
-//                   (alpha bits and key) to the segment's start; norm partials
+//   k_alpha         Markov alpha (reference double order), flat over the
+//                   candidates: a seen candidate's count is replaced in place by
+//                   its alpha bits (an unseen one keeps count 0: alpha -1);
+//                   survivors counted per segment; norm partials
 //   scan            -> output offset of every segment
 //   k_norm          per-proteome norm, scale, nnz
 //   (host reads nnz, checks capacity)
-//   k_compact       survivors' keys and normalised values, copied segment by segment
+//   k_compact       survivors' keys and normalised values, segment by segment
 //   k_union_mark    (with a key bitmap) the candidate keys of every seen (K-1)-mer
 #include "cv_build.cuh"
 #include "hostctx.cuh"
