@@ -481,9 +481,11 @@ cudaError_t compare_launch(cudaStream_t stream, void *scratch, size_t scratch_si
         return cudaSuccess;
     }
     PHYLO_CHECK(compare_attributes());
-    // about three CTAs per SM, at most CMP_MAX_RUN tiles each
+    // two CTAs per SM (three fit): one pair's split searches and the last CTA's
+    // combine cost less over fewer, longer runs (synchronous call on 6.6 M entries:
+    // 0.045 ms against 0.053 with three); at most CMP_MAX_RUN tiles each
     const uint32_t sms = (uint32_t)device_sm_count();
-    uint32_t grid = min(ntiles, min(3u * sms, CMP_MIN_CAP));
+    uint32_t grid = min(ntiles, min(2u * sms, CMP_MIN_CAP));
     uint32_t per = (uint32_t)div_up(ntiles, grid);
     if (per > CMP_MAX_RUN) per = CMP_MAX_RUN;
     grid = (uint32_t)div_up(ntiles, per);
