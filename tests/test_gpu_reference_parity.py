@@ -211,3 +211,69 @@ def test_compare_full_size_vectors(ref, bufs):
             assert abs(c_ours - exact) <= 1e-12
             checked += 1
     assert checked >= 10
+
+
+def test_plain_path_timing_against_the_reference(ref, bufs):
+    """The reference's own library and this one, timed on the same GB300 through the
+    same synchronous calls (the plain per-proteome / per-pair path Rocket drives):
+    buildCompositionVector on a full-size proteome (1,500 proteins, K = 6) and
+    compareCompositionVectors on two of its vectors.  Prints both; this library must
+    not be slower."""
+    import time
+    uni = synth.workload("uniform256", n=2)
+    seqs = [uni.get(0), uni.get(1)]
+    st = torch.cuda.current_stream().cuda_stream
+    max_size = 8 * max(len(s) for s in seqs) + 4096
+    d_in = [to_device_bytes(s) for s in seqs]
+    keys = [torch.empty(max_size, dtype=torch.int32, device="cuda") for _ in range(4)]
+    vals = [torch.empty(max_size, dtype=torch.float32, device="cuda") for _ in range(4)]
+    size = np.zeros(1, np.int32)
+    rs = bufs.ref_scratch("protein", 6, max_size)
+    os_ = bufs.our_scratch("protein", 6, max_size)
+
+    def build(who, i, slot):
+        if who == "ref":
+            rc = refabi.build(st, rs, "protein", 6, d_in[i], len(seqs[i]), keys[slot],
+                              vals[slot], size, max_size)
+        else:
+            rc = Bindings.INSTANCE.buildCompositionVector(
+                st, os_.data_ptr(), os_.numel(), "protein", 6, d_in[i].data_ptr(), len(seqs[i]),
+                keys[slot].data_ptr(), vals[slot].data_ptr(), size, max_size)
+        assert rc == 0
+        return int(size[0])
+
+    n = {}
+    for who, base in (("ref", 0), ("ours", 2)):
+        for i in range(2):
+            n[(who, i)] = build(who, i, base + i)
+    t = {}
+    for who, base in (("ref", 0), ("ours", 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            build(who, 0, base)
+        t[("build", who)] = (time.perf_counter() - t0) / 5
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for who, base in (("ref", 0), ("ours", 2)):
+        nl, nr = n[(who, 0)], n[(who, 1)]
+        if who == "ref" and refabi.compare_block_race(nl, nr):
+            pytest.skip("these sizes race in the reference's compare")
+        args = (keys[base], vals[base], nl, keys[base + 1], vals[base + 1], nr)
+        for rep in range(21):
+            if rep == 1:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+            if who == "ref":
+                rc = refabi.compare(st, rs, args[0], args[1], nl, args[3], args[4], nr, out)
+            else:
+                rc = Bindings.INSTANCE.compareCompositionVectors(
+                    st, os_.data_ptr(), os_.numel(), args[0].data_ptr(), args[1].data_ptr(), nl,
+                    args[3].data_ptr(), args[4].data_ptr(), nr, out.data_ptr())
+            assert rc == 0
+        t[("compare", who)] = (time.perf_counter() - t0) / 20
+    print(f"\nplain path on this GPU, {n[('ours', 0)]:,} + {n[('ours', 1)]:,} entries: "
+          f"build {1000 * t[('build', 'ref')]:.2f} ms (reference) vs "
+          f"{1000 * t[('build', 'ours')]:.2f} ms; compare {1000 * t[('compare', 'ref')]:.3f} ms "
+          f"(reference) vs {1000 * t[('compare', 'ours')]:.3f} ms")
+    assert t[("build", "ours")] <= t[("build", "ref")]
+    assert t[("compare", "ours")] <= t[("compare", "ref")]
