@@ -172,21 +172,24 @@ def _barrier_max(value: float, world: int) -> float:
 # CPU baseline (the reference's CPU path, restated in C under oracle/)
 # ----------------------------------------------------------------------------
 
-def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed=0, k=6):
-    """Times buildCPU on a seeded sample of proteomes and compareCPU on pairs of
-    them for about `seconds`, and extrapolates to the whole workload."""
+def cpu_baseline(wl, n_pairs_total, n_build_total, seconds=15.0, threads=0, seed=0, k=6,
+                 n_sample=0):
+    """Times buildCPU on a seeded sample of proteomes (n_sample, default one per
+    thread and at least 4) and compareCPU on pairs of them for about `seconds`, and
+    extrapolates to the whole workload."""
     from oracle import oracle as O
     O.lib()
     threads = threads or O.max_threads()
     rng = np.random.default_rng(seed)
-    nb = min(len(wl), max(threads, 4))
+    nb = min(len(wl), n_sample or max(threads, 4))
     ids = rng.choice(len(wl), nb, replace=False)
     t_start = time.perf_counter()
     t0 = time.perf_counter()
     vecs = O.java_build_many([wl.get(int(i)) for i in ids], k, threads=threads)
     t_build = time.perf_counter() - t0
     build_rate = nb / t_build                                      # proteomes / s
-    pairs = [(a, b) for a in range(nb) for b in range(a + 1, nb)]
+    # (one sampled proteome: its vector against itself)
+    pairs = [(a, b) for a in range(nb) for b in range(a + 1, nb)] or [(0, 0)]
     budget = max(1.0, seconds - t_build)
     done, t_cmp = 0, 0.0
     while t_cmp < budget and done < 100000:
@@ -589,6 +592,10 @@ def run_ours(args):
         cb = cpu_baseline(wl, n_pairs, N, seconds=args.ref_seconds, k=args.k)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample",
                                                    "extrapolated")}
+        # the same port on one thread (a bounded sample: one proteome, compared with itself)
+        c1 = cpu_baseline(wl, n_pairs, N, seconds=2.0, threads=1, k=args.k, n_sample=1)
+        line["cpu_baseline"]["single_thread"] = {k: c1[k] for k in ("value", "unit", "cores",
+                                                                    "sample", "extrapolated")}
     if not args.no_serve and world == 1:
         del engine, arena, builder, out, flush, seq
         torch.cuda.synchronize()
