@@ -562,7 +562,11 @@ __global__ void k_cand_bases(BuildArgs a) {
 }
 
 // Every K-window adds one to the slot of its candidate (native.cu:244); with
-// compact (K-1)-mer tables every (K-1)-window also adds one to its count.
+// compact (K-1)-mer tables every (K-1)-window also adds one to its count.  A
+// thread's windows go through the dependent steps together (codes, rank loads,
+// counts, offsets and masks, slot atomics), so their loads are in flight at once.
+// The L2 atomics, not those loads, set the pace: the same kernel with four windows
+// per thread instead of two measured no faster.
 __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
     __shared__ uint8_t dig[TILE + 16];
     const int K = a.k;
@@ -578,36 +582,65 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_c0_scatter(BuildArgs a) {
         }
         __syncthreads();
         const uint64_t cbase = a.cbase[p];
-        for (int u = 0; u < TILE / COUNT_THREADS; u++) {
+        constexpr int NU = TILE / COUNT_THREADS;
+        // phase 1: every window's (K-1)- and (K-2)-mer codes from the staged digits
+        uint32_t w[NU], w2[NU], bd[NU];
+        int jj[NU];
+#pragma unroll
+        for (int u = 0; u < NU; u++) {
             const int li = u * COUNT_THREADS + threadIdx.x;
-            bool v0 = false;
-            uint64_t slot = 0;
+            w[u] = 0;
+            w2[u] = 0;
+            bd[u] = 0xffu;
+            jj[u] = -1;
             if (start + li < len) {
-                uint32_t w = 0, w2 = 0;
+                uint32_t x = 0, x2 = 0;
                 int j;
                 for (j = 0; j < K - 1; j++) {
-                    if (j == K - 2) w2 = w;  // the first K-2 symbols
+                    if (j == K - 2) x2 = x;
                     uint32_t d = dig[li + j];
                     if (d == 0xffu) break;
-                    w = w * A + d;
+                    x = x * A + d;
                 }
-                if (a.compact2 && j >= K - 2) {  // a (K-2)-window starts here: its count
-                    const uint64_t mi = c2_index(a, p, w2);
-                    if (mi < a.cap2) atomicAdd(&a.c2[mi], 1u);
-                }
-                if (j == K - 1) {
-                    const uint64_t wi = c1_index(a, p, w);
-                    const bool in_cap = !a.compact1 || wi < a.cap1;
-                    if (a.compact1 && in_cap) atomicAdd(&a.c1[wi], 1u);  // (K-1)-window count
-                    uint32_t b = dig[li + K - 1];
-                    if (b != 0xffu && in_cap) {
-                        v0 = true;
-                        uint32_t m = a.fdT2.mod(w);
-                        slot = cbase + a.coff[wi] + __popc(ext_mask(a, p, m) & ((1u << b) - 1u));
-                    }
-                }
+                w[u] = x;
+                w2[u] = x2;
+                jj[u] = j;
+                bd[u] = dig[li + K - 1];
             }
-            if (v0 && slot < a.cand_cap) atomicAdd(&a.c0a[slot], 1u);
+        }
+        // phase 2: all rank loads in flight together
+        uint64_t wi[NU], mi[NU];
+#pragma unroll
+        for (int u = 0; u < NU; u++) {
+            wi[u] = jj[u] == K - 1 ? c1_index(a, p, w[u]) : ~0ull;
+            mi[u] = (a.compact2 && jj[u] >= K - 2) ? c2_index(a, p, w2[u]) : ~0ull;
+        }
+        // phase 3: counts, then the candidate offsets and extension masks together
+        uint32_t co[NU], em[NU];
+#pragma unroll
+        for (int u = 0; u < NU; u++) {
+            co[u] = 0;
+            em[u] = 0;
+            if (mi[u] < a.cap2) atomicAdd(&a.c2[mi[u]], 1u);
+            if (wi[u] != ~0ull) {
+                const bool in_cap = !a.compact1 || wi[u] < a.cap1;
+                if (a.compact1 && in_cap) atomicAdd(&a.c1[wi[u]], 1u);
+                if (!in_cap || bd[u] == 0xffu) wi[u] = ~0ull;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < NU; u++) {
+            if (wi[u] != ~0ull) {
+                co[u] = __ldg(&a.coff[wi[u]]);
+                em[u] = ext_mask(a, p, a.fdT2.mod(w[u]));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < NU; u++) {
+            if (wi[u] != ~0ull) {
+                const uint64_t slot = cbase + co[u] + __popc(em[u] & ((1u << bd[u]) - 1u));
+                if (slot < a.cand_cap) atomicAdd(&a.c0a[slot], 1u);
+            }
         }
         __syncthreads();
     }
