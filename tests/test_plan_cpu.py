@@ -196,3 +196,46 @@ def test_item_cost_models_split_tile_estimates():
         np.testing.assert_allclose(sums, whole[name], rtol=1e-12)
     # the window kernel's launch order follows its own (linear) estimate
     np.testing.assert_allclose(plan.est, m["linear"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("algorithm", ["window", "postings"])
+@pytest.mark.parametrize("diagonal", [True, False])
+def test_nonfinite_vectors_recomputed_pairs(algorithm, diagonal):
+    """Pairs with a vector whose norm is not finite (a proteome without K-windows)
+    are recomputed by the merge path: exactly those pairs of the plan (the self
+    products only when the diagonal is asked for), written to both mirror slots."""
+    import torch
+    n = 40
+    eng = _engine(_nnz(n, 8), R=16, algorithm=algorithm, block=64, tile_rows=16,
+                  tile_cols=128)
+    norms = np.ones(n)
+    bad = [3, 17, 39]
+    norms[bad] = np.nan
+    eng.arena.norms = norms
+    plan = eng.plan_triangle(ldc=n)
+    calls = []
+
+    def fake_merge(pa, pb, col_arena=None, stream=None):
+        calls.append((pa.copy(), pb.copy()))
+        return torch.from_numpy(1000.0 + pa * n + pb)
+
+    eng.compare_pairs_merge = fake_merge
+    out = torch.full((n * n,), -1.0, dtype=torch.float64)
+    eng._fix_nonfinite(plan, out, None, diag=diagonal)
+    (pa, pb), = calls
+    got = {(int(a), int(b)) for a, b in zip(pa, pb)}
+    assert len(got) == len(pa)  # each pair once
+    want = set()
+    for i in range(n):
+        for j in range(i, n):
+            if (i in bad or j in bad) and (i != j or diagonal):
+                want.add((i, j))
+    assert {(min(a, b), max(a, b)) for a, b in got} == want
+    o = out.view(n, n).numpy()
+    for a, b in got:
+        assert o[a, b] == o[b, a] == 1000.0 + a * n + b
+    assert np.count_nonzero(o != -1.0) == 2 * len(want) - sum(1 for a, b in want if a == b)
+    # nothing to do when every norm is finite
+    eng.arena.norms = np.ones(n)
+    eng._fix_nonfinite(plan, out, None, diag=diagonal)
+    assert len(calls) == 1
