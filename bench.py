@@ -358,6 +358,8 @@ def run_reference(args):
 BENCH_TUNE_SPACE = [
     dict(algorithm="window", wshift=11, tile_rows=16, tile_cols=256, fold=28, items_per_cta=16),
     dict(algorithm="window", wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=16),
+    dict(algorithm="window", wshift=11, tile_rows=16, tile_cols=256, fold=28, items_per_cta=8),
+    dict(algorithm="window", wshift=11, tile_rows=16, tile_cols=128, fold=28, items_per_cta=8),
     dict(algorithm="postings", block=128, wshift=9, items_per_cta=4),
     dict(algorithm="postings", block=64, wshift=9, items_per_cta=4),
 ]
