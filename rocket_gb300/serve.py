@@ -75,7 +75,7 @@ class Budget:
 
     def reserve(self, nbytes: float, timeout: float = 600.0) -> None:
         with self.cv:
-            if nbytes > self.total - self.used and self.used == 0:
+            if nbytes > self.total:  # would never fit, however much is released
                 raise MemoryError(f"request needs {nbytes / 1e9:.1f} GB, budget {self.total / 1e9:.1f} GB")
             ok = self.cv.wait_for(lambda: self.used + nbytes <= self.total, timeout=timeout)
             if not ok:
@@ -309,8 +309,9 @@ class ServingEngine:
         reserved = 0.0
         try:
             db_n = self.db.snapshot()
-            reserved = self._estimate(reqs, db_n)
-            self.budget.reserve(reserved)
+            need = self._estimate(reqs, db_n)
+            self.budget.reserve(need)
+            reserved = need  # released below only once actually reserved
             t0 = time.perf_counter()
             for r in reqs:
                 r.t_start = t0
