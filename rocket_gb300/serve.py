@@ -22,7 +22,8 @@ builds items into device cache slots and correlates pairs of resident items
   same order whether its query ran alone or with others.
 * Appends copy the staged vectors into the database arena (preallocated to its
   share of the budget, so concurrent batches reading older entries are never
-  disturbed) and extend the window index; a later batch's snapshot includes them.
+  disturbed) and extend the window index; a later batch's snapshot includes them
+  once those copies have completed on the device.
 """
 from __future__ import annotations
 
@@ -111,13 +112,24 @@ class Database:
         self.lock = threading.Lock()
         self.appended = 0
         self.refused = 0
+        self.visible = 0  # vectors a batch may read: their copies have completed
+        # (vector count after an append, event recorded behind that append's copies),
+        # in append order
+        self.pending: collections.deque = collections.deque()
 
     def bytes_reserved(self) -> float:
         return self.capacity_entries * 8.0 + self.capacity_vectors * (self.R + 1) * 4.0
 
     def snapshot(self) -> int:
+        """Vectors a new batch compares against.  An append's vectors count only once
+        its copies have completed on the device: they are queued on the appending
+        slot's stream behind that slot's own pair kernel, while a batch of another
+        slot runs on its own stream and would otherwise read entries, offsets and
+        window rows still in flight."""
         with self.lock:
-            return self.arena.n
+            while self.pending and self.pending[0][1].query():
+                self.visible = self.pending.popleft()[0]
+            return self.visible
 
     def append(self, staged: Arena, stream: torch.cuda.Stream) -> bool:
         """Copies the staged vectors (built and indexed) behind the current ones."""
@@ -136,6 +148,9 @@ class Database:
                                                       non_blocking=True)
                 # window offsets are relative to each vector's start: copied as is
                 a.roff[a.n:a.n + n_new].copy_(staged.roff[:n_new], non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(stream)
+            self.pending.append((a.n + n_new, done))
             a.nnz = np.concatenate([a.nnz, staged.nnz[:n_new]])
             a.norms = np.concatenate([a.norms, staged.norms[:n_new]])
             a.off = np.concatenate([a.off[:a.n + 1], base + staged.off[1:n_new + 1]])

@@ -150,3 +150,64 @@ def test_failed_admission_releases_nothing():
     assert all(r.done.is_set() and "MemoryError" in r.error for r in reqs)
     assert srv.budget.used == 30.0
     assert not slot.busy and srv.completed == reqs
+
+
+# -- appends become visible only once their copies have completed -------------------
+
+import torch  # noqa: E402
+
+from rocket_gb300.engine import Arena, EngineConfig  # noqa: E402
+from rocket_gb300.serve import Database  # noqa: E402
+
+
+class _CopyDone:
+    """Stands in for the CUDA event recorded behind an append's copies."""
+    made = []
+
+    def __init__(self):
+        self.done = False
+        _CopyDone.made.append(self)
+
+    def record(self, stream=None):
+        pass
+
+    def query(self):
+        return self.done
+
+
+def _staged(nnz, R):
+    off = np.concatenate([[0], np.cumsum(nnz)]).astype(np.int64)
+    used = int(off[-1])
+    keys = torch.arange(used, dtype=torch.int32)
+    vals = torch.ones(used, dtype=torch.float32)
+    return Arena("protein", 3, keys, vals, torch.from_numpy(off.copy()),
+                 np.asarray(nnz, np.int64), off, np.ones(len(nnz)), n=len(nnz),
+                 roff=torch.zeros((len(nnz), R + 1), dtype=torch.int32), R=R, indexed=len(nnz))
+
+
+def test_appends_visible_after_their_copies(monkeypatch):
+    """A batch's snapshot counts an append's vectors only once the copies queued
+    behind the appending slot's work have completed, and in append order: a later
+    append that completes first waits for the earlier one."""
+    monkeypatch.setattr(torch.cuda, "Event", _CopyDone)
+    _CopyDone.made = []
+    db = Database("protein", 3, 1000, 10, EngineConfig(segments=4, compress=False), "cpu")
+    assert db.append(_staged([4, 8], db.R), None)
+    assert db.arena.n == 2 and db.snapshot() == 0  # copies in flight
+    first, = _CopyDone.made
+    first.done = True
+    assert db.snapshot() == 2
+    assert db.append(_staged([12], db.R), None)
+    assert db.append(_staged([4, 4, 4], db.R), None)
+    second, third = _CopyDone.made[1:]
+    third.done = True
+    assert db.arena.n == 6 and db.snapshot() == 2  # the earlier append is still in flight
+    second.done = True
+    assert db.snapshot() == 6
+    # the arena holds the vectors in append order, each on its own offsets
+    assert list(db.arena.off) == [0, 4, 12, 24, 28, 32, 36]
+    assert list(db.arena.vec_off[:7].numpy()) == list(db.arena.off)
+    assert list(db.arena.nnz) == [4, 8, 12, 4, 4, 4]
+    # over capacity: refused, nothing published
+    assert not db.append(_staged([4] * 5, db.R), None)
+    assert db.refused == 5 and db.snapshot() == 6 and len(_CopyDone.made) == 3
