@@ -289,6 +289,12 @@ class BatchBuilder:
                 arena.values = _grow(arena.values, cap)
                 if arena.rkeys is not None:
                     arena.rkeys = None
+                if st is not stream:
+                    # the copies into the new buffers run on the build's stream and
+                    # cover the range this batch's emit (on the side stream) writes
+                    grown = torch.cuda.Event()
+                    grown.record(stream)
+                    st.wait_event(grown)
             # mark the union bitmap for dense key ranks while every vector is marked
             mark = arena.union_n == arena.n
             if mark and arena.union_bits is None:

@@ -195,6 +195,25 @@ def test_batched_build_equals_single_and_counts():
     assert np.array_equal(k1, e1) and np.array_equal(k2, e2) and tuple(tot) == et
 
 
+def test_batched_build_grows_a_small_arena():
+    """An arena too small for the build grows while two batches are in flight (each
+    growth copies the old buffers on the build's stream, and the next emit may run on
+    the side stream): the vectors equal those of a build into a fresh arena."""
+    p = synth.workload("uneven1024", n=7, scale=0.03)
+    d = torch.from_numpy(p.data).cuda()
+    ref = BatchBuilder("protein", 6, max_batch=2).build(d, p.offsets)
+    b = BatchBuilder("protein", 6, max_batch=2)  # four batches, two in flight
+    small = b.new_arena(64, 7)
+    got = b.build(d, p.offsets, arena=small)
+    torch.cuda.synchronize()
+    assert got.n == ref.n == 7 and got.keys.numel() > 64
+    assert np.array_equal(got.off, ref.off) and np.array_equal(got.nnz, ref.nnz)
+    for i in range(7):
+        k0, v0 = ref.host_vector(i)
+        k1, v1 = got.host_vector(i)
+        assert np.array_equal(k0, k1) and np.array_equal(v0.view(np.uint32), v1.view(np.uint32))
+
+
 def test_batched_counts_k7_compact_tables():
     """Protein K = 7 keeps both the (K-1)- and the (K-2)-mer counts compact (one
     entry per seen (K-1)- / (K-2)-mer of the batch); phyloBuildBatchCounts expands
