@@ -8,11 +8,11 @@ correlateGPU for every pair; rocket/scheduler/DeviceWorker.java:118-323):
   device arena (keys | values | offsets), vectors padded to 4 entries so the
   pair kernel can read them with 16-byte loads.
 * :class:`PairEngine` compares every pair of an arena (or a rectangle of row
-  and column vectors).  Two algorithms: ``postings`` (csrc/postings.cu, the
-  default) regroups each key window of a block of row vectors and a block of
-  column vectors by key and forms only the products of shared keys, with exact
-  integer sums; ``window`` (csrc/allpairs.cu) densifies 16 row vectors per key
-  window in shared memory and streams column vectors against them.  The planner
+  and column vectors).  Two algorithms: ``window`` (csrc/allpairs.cu, the
+  default) densifies 16 row vectors per key window in shared memory and streams
+  column vectors against them; ``postings`` (csrc/postings.cu) regroups each key
+  window of a block of row vectors and a block of column vectors by key and forms
+  only the products of shared keys, with exact integer sums.  The planner
   sorts vectors by size, cuts the pair matrix into tiles and the key space into
   segments, estimates each item's cost (for postings from the products of the
   tile's vector sizes) and hands items out longest first.
@@ -781,12 +781,11 @@ class PairEngine:
 
     # -- merge-path algorithm over explicit pairs -------------------------------
     def _nnz_dev(self, arena: Arena) -> torch.Tensor:
-        key = id(arena), arena.n
-        cache = getattr(self, "_nnz_cache", {})
-        if key not in cache:
-            cache[key] = torch.from_numpy(arena.nnz[:arena.n].astype(np.int32)).to(self.device)
-            self._nnz_cache = cache
-        return cache[key]
+        """The arena's entry counts on the device, copied on every call (a few KB):
+        an arena object is reset and rebuilt in place (a serving slot's query
+        arena), so neither its identity nor its size says its counts are unchanged.
+        Allocated on the current stream, which the caller's kernels use."""
+        return torch.from_numpy(arena.nnz[:arena.n].astype(np.int32)).to(self.device)
 
     def compare_pairs_merge(self, pa, pb, col_arena: Optional[Arena] = None, stream=None,
                             out: Optional[torch.Tensor] = None) -> torch.Tensor:
@@ -810,10 +809,12 @@ class PairEngine:
         with torch.cuda.stream(s_obj):
             dpa = torch.from_numpy(pa.astype(np.int32)).to(self.device, non_blocking=True)
             dpb = torch.from_numpy(pb.astype(np.int32)).to(self.device, non_blocking=True)
+            na = self._nnz_dev(a)
+            nb = na if ca is a else self._nnz_dev(ca)
         check(self.L.phyloComparePairsMany(
             int(s_obj.cuda_stream), _p(self._many_scratch), self._many_scratch.numel(),
-            _p(a.keys), _p(a.values), _p(a.vec_off), _p(self._nnz_dev(a)),
-            _p(ca.keys), _p(ca.values), _p(ca.vec_off), _p(self._nnz_dev(ca)),
+            _p(a.keys), _p(a.values), _p(a.vec_off), _p(na),
+            _p(ca.keys), _p(ca.values), _p(ca.vec_off), _p(nb),
             _p(dpa), _p(dpb), P, tiles, _p(out)))
         self.launches += 7
         return out
