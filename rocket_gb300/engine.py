@@ -784,8 +784,10 @@ class PairEngine:
         """The arena's entry counts on the device, copied on every call (a few KB):
         an arena object is reset and rebuilt in place (a serving slot's query
         arena), so neither its identity nor its size says its counts are unchanged.
-        Allocated on the current stream, which the caller's kernels use."""
-        return torch.from_numpy(arena.nnz[:arena.n].astype(np.int32)).to(self.device)
+        Allocated and copied on the current stream, which the caller's kernels use
+        (from pageable memory: staged before the call returns, like the pair lists)."""
+        return torch.from_numpy(arena.nnz[:arena.n].astype(np.int32)).to(self.device,
+                                                                          non_blocking=True)
 
     def compare_pairs_merge(self, pa, pb, col_arena: Optional[Arena] = None, stream=None,
                             out: Optional[torch.Tensor] = None) -> torch.Tensor:
