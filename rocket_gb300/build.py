@@ -14,6 +14,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphylogenetics.so")
 SYNTH_LIB = os.path.join(HERE, "libphylo_synth.so")
@@ -56,6 +57,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     build_synth(force)
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    if os.path.isdir(INCLUDE):  # the C ABI header capi.cu includes
+        headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
