@@ -76,3 +76,54 @@ def test_batch_scratch_rejects_bad_arguments(lib):
     assert lib.phyloPairsThreads(10, 32, 64) == 512 and lib.phyloPairsThreads(9, 32, 64) == 256
     assert lib.phyloPairsThreads(10, 16, 64) == 256 and lib.phyloPairsThreads(9, 16, 32) == 128
     assert lib.phyloPairsThreads(11, 16, 128) == 512
+
+
+def _prototypes():
+    """(return type, name, [parameter types]) of every function the header declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = []
+    for ret, name, args in re.findall(
+            r"^\s*((?:unsigned\s+)?(?:long|int|void))\s+(\w+)\s*\(([^)]*)\)\s*;", text, flags=re.M):
+        params = []
+        for a in args.split(","):
+            a = " ".join(a.split())
+            if a in ("", "void"):
+                continue
+            params.append(re.sub(r"\s*\b\w+$", "", a).strip())
+        out.append((ret, name, params))
+    return out
+
+
+def _ctype_ok(c_type: str, declared) -> bool:
+    """Whether the ctypes declaration passes the C type with the same width and
+    register class (LP64: long and pointers are 64-bit; addresses may be passed
+    as uintptr_t-sized integers)."""
+    if c_type == "int":
+        return declared is ctypes.c_int
+    if c_type == "unsigned int":
+        return declared is ctypes.c_uint
+    if c_type == "long":
+        return declared is ctypes.c_long
+    if c_type == "const char *":
+        return declared is ctypes.c_char_p
+    if c_type == "uintptr_t" or c_type.endswith("*"):
+        return declared is ctypes.c_size_t or (
+            isinstance(declared, type) and issubclass(declared, ctypes._Pointer))
+    raise AssertionError(f"no rule for C type {c_type!r}")
+
+
+def test_ctypes_declarations_match_the_header(lib):
+    """Every prototype in include/phylogenetics.h and the ctypes declaration the
+    Python side calls it through agree on the parameter count and on each
+    parameter's and the result's width."""
+    protos = _prototypes()
+    assert sorted(n for _, n, _ in protos) == sorted(_native.EXPORTED)
+    rets = {"int": ctypes.c_int, "long": ctypes.c_long, "void": None}
+    for ret, name, params in protos:
+        f = getattr(lib, name)
+        assert f.restype is rets[ret], name
+        assert len(f.argtypes) == len(params), (name, len(f.argtypes), len(params))
+        for i, (c_type, declared) in enumerate(zip(params, f.argtypes)):
+            assert _ctype_ok(c_type, declared), (name, i, c_type, declared)
