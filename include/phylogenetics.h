@@ -11,7 +11,10 @@
  *     the library never allocates, frees or selects a device;
  *   - the return value is a cudaError_t code (0 = cudaSuccess); argument
  *     errors print a message on stderr and return cudaErrorUnknown (999),
- *     except where stated.
+ *     except where stated;
+ *   - a negative count or byte size (vector lengths, scratch sizes, numbers
+ *     of vectors, items, tiles or pairs) returns cudaErrorInvalidValue (1)
+ *     before any device work; the size queries (long results) return -1.
  */
 #ifndef ROCKET_GB300_PHYLOGENETICS_H
 #define ROCKET_GB300_PHYLOGENETICS_H

@@ -128,9 +128,12 @@ int buildCompositionVector(uintptr_t stream, uintptr_t d_temp_storage_ptr, long 
                 alphabet);
         return (int)cudaErrorUnknown;
     }
-    if (string_len < 0 || (uint64_t)string_len > 0xffffffffull || max_vector_size < 0) {
-        fprintf(stderr, "error: invalid sizes (string_len=%ld, max_vector_size=%d)\n", string_len,
-                max_vector_size);
+    if (string_len < 0 || (uint64_t)string_len > 0xffffffffull || max_vector_size < 0 ||
+        temp_storage_size < 0) {
+        fprintf(stderr,
+                "error: invalid sizes (string_len=%ld, max_vector_size=%d, "
+                "temp_storage_size=%ld)\n",
+                string_len, max_vector_size, temp_storage_size);
         return (int)cudaErrorInvalidValue;
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -185,8 +188,9 @@ int compareCompositionVectors(uintptr_t stream, uintptr_t d_temp_storage_ptr, lo
                               uintptr_t d_left_keys_ptr, uintptr_t d_left_values_ptr, int left_size,
                               uintptr_t d_right_keys_ptr, uintptr_t d_right_values_ptr,
                               int right_size, uintptr_t d_output_ptr) {
-    if (left_size < 0 || right_size < 0) {
-        fprintf(stderr, "error: negative vector size (%d, %d)\n", left_size, right_size);
+    if (left_size < 0 || right_size < 0 || temp_storage_size < 0) {
+        fprintf(stderr, "error: negative size (vectors %d, %d; scratch %ld)\n", left_size,
+                right_size, temp_storage_size);
         return (int)cudaErrorInvalidValue;
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -261,7 +265,8 @@ int phyloBuildBatchPlan(uintptr_t stream, uintptr_t d_scratch, long scratch_size
                         int64_t *h_candidates) {
     const int alpha = parse_alphabet(alphabet);
     BuildGeometry g;
-    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0) {
+    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0 ||
+        max_candidates < 0 || scratch_size < 0) {
         fprintf(stderr, "error: invalid batch build arguments (alphabet %s, k=%d, n=%d)\n",
                 alphabet ? alphabet : "(null)", k, num_proteomes);
         return (int)cudaErrorInvalidValue;
@@ -297,7 +302,8 @@ int phyloBuildBatchPlanAsync(uintptr_t stream, uintptr_t d_scratch, long scratch
                              uintptr_t d_seq_off, long max_candidates, void *h_summary) {
     const int alpha = parse_alphabet(alphabet);
     BuildGeometry g;
-    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0 || !h_summary) {
+    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0 || !h_summary ||
+        max_candidates < 0 || scratch_size < 0) {
         fprintf(stderr, "error: invalid batch build arguments (alphabet %s, k=%d, n=%d)\n",
                 alphabet ? alphabet : "(null)", k, num_proteomes);
         return (int)cudaErrorInvalidValue;
@@ -334,7 +340,8 @@ int phyloBuildBatchEmit(uintptr_t stream, uintptr_t d_scratch, long scratch_size
                         long arena_base, uintptr_t d_union_bits) {
     const int alpha = parse_alphabet(alphabet);
     BuildGeometry g;
-    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0)
+    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0 ||
+        max_candidates < 0 || scratch_size < 0 || arena_base < 0)
         return (int)cudaErrorInvalidValue;
     cudaStream_t st = (cudaStream_t)stream;
     BuildArgs a;
@@ -360,7 +367,8 @@ int phyloBuildBatchNorms(uintptr_t stream, uintptr_t d_scratch, long scratch_siz
                          double *h_norms) {
     const int alpha = parse_alphabet(alphabet);
     BuildGeometry g;
-    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0)
+    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || num_proteomes <= 0 ||
+        max_candidates < 0 || scratch_size < 0 || !h_norms)
         return (int)cudaErrorInvalidValue;
     BuildArgs a;
     memset(&a, 0, sizeof(a));
@@ -414,7 +422,8 @@ int phyloBuildBatchCounts(uintptr_t stream, uintptr_t d_scratch, long scratch_si
                           int p, uint32_t *h_c1, uint32_t *h_c2, uint32_t *h_tot) {
     const int alpha = parse_alphabet(alphabet);
     BuildGeometry g;
-    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || p < 0 || p >= num_proteomes)
+    if (alpha < 0 || build_geometry(alpha, k, &g) != 0 || p < 0 || p >= num_proteomes ||
+        max_candidates < 0 || scratch_size < 0 || !h_c1 || !h_c2 || !h_tot)
         return (int)cudaErrorInvalidValue;
     BuildArgs a;
     memset(&a, 0, sizeof(a));
@@ -449,6 +458,8 @@ int phyloBuildLaunchesPerBatch(void) { return build_launches_per_batch(); }
 int phyloWindowIndex(uintptr_t stream, uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors,
                      int window_shift, unsigned int num_windows, long max_vector_len,
                      uintptr_t d_roff) {
+    if (num_vectors < 0 || window_shift < 0 || window_shift > 31 || max_vector_len < 0)
+        return (int)cudaErrorInvalidValue;
     return (int)range_index_launch((const uint32_t *)d_keys, (const uint64_t *)d_vec_off,
                                    (uint32_t)num_vectors, num_windows, (uint32_t)window_shift,
                                    (uint32_t *)d_roff, (cudaStream_t)stream,
@@ -486,7 +497,7 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
                      uintptr_t d_part, int fold, uintptr_t d_item_cycles, int tile_rows,
                      int tile_cols, int grid) {
     if (!ap_shape_ok(tile_rows, tile_cols) || window_shift < 4 ||
-        window_shift > ap_max_wshift(tile_rows, tile_cols))
+        window_shift > ap_max_wshift(tile_rows, tile_cols) || num_items < 0 || grid <= 0)
         return (int)cudaErrorInvalidValue;
     ApArgs a;
     a.row.keys = (const uint32_t *)d_row_keys;
@@ -515,7 +526,9 @@ int phyloPairsLaunch(uintptr_t stream, uintptr_t d_row_keys, uintptr_t d_row_val
 int phyloPairsReduce(uintptr_t stream, uintptr_t d_part, uintptr_t d_tiles, int num_tiles,
                      int segments, int tile_rows, int tile_cols, uintptr_t d_rowids,
                      uintptr_t d_colids, uintptr_t d_out, long ldc, int upper, int mirror) {
-    if (!ap_shape_ok(tile_rows, tile_cols) || upper < 0 || upper > 2) return (int)cudaErrorInvalidValue;
+    if (!ap_shape_ok(tile_rows, tile_cols) || upper < 0 || upper > 2 || num_tiles < 0 ||
+        (num_tiles > 0 && segments <= 0) || ldc <= 0)
+        return (int)cudaErrorInvalidValue;
     ApReduceArgs r;
     r.part = (const FF *)d_part;
     r.tiles = (const ApTile *)d_tiles;
@@ -618,7 +631,7 @@ long phyloKeyRankBitmapBytes(long key_limit) {
 int phyloKeyRanks(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes, long key_limit,
                   uintptr_t d_keys, uintptr_t d_vec_off, int num_vectors, long max_vector_len,
                   uintptr_t d_union_bits, uintptr_t d_rank_keys, uintptr_t d_union_size) {
-    if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0 ||
+    if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0 || max_vector_len < 0 ||
         scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit))
         return (int)cudaErrorInvalidValue;
     return (int)key_ranks((const uint32_t *)d_keys, (const uint64_t *)d_vec_off,
@@ -632,7 +645,7 @@ int phyloKeyRankIndex(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes,
                       long arena_entries, uintptr_t d_union_bits, int window_shift,
                       unsigned int num_windows, uintptr_t d_rank_keys, uintptr_t d_roff) {
     if (key_limit <= 0 || key_limit > 0xffffffffl || num_vectors < 0 || window_shift < 0 ||
-        window_shift > 31 || arena_entries < 0 ||
+        window_shift > 31 || arena_entries < 0 || max_vector_len < 0 ||
         scratch_bytes < (long)rank_scratch_bytes((uint64_t)key_limit))
         return (int)cudaErrorInvalidValue;
     return (int)key_rank_index((const uint32_t *)d_keys, (const uint64_t *)d_vec_off,
@@ -645,18 +658,21 @@ int phyloKeyRankIndex(uintptr_t stream, uintptr_t d_scratch, long scratch_bytes,
 
 int phyloSelfDot(uintptr_t stream, uintptr_t d_values, uintptr_t d_vec_off, int num_vectors,
                  long max_vector_len, uintptr_t d_part, uintptr_t d_out, long ldc) {
+    if (num_vectors < 0 || max_vector_len < 0 || ldc <= 0) return (int)cudaErrorInvalidValue;
     return (int)self_dot_launch((const float *)d_values, (const uint64_t *)d_vec_off,
                                 (uint32_t)num_vectors, (double *)d_out, (uint64_t)ldc,
                                 (uint64_t)max_vector_len, (FF *)d_part, (cudaStream_t)stream);
 }
 
 long phyloSelfDotPartBytes(int num_vectors, long max_vector_len) {
+    if (num_vectors < 0 || max_vector_len < 0) return -1;
     return (long)(self_dot_part_count((uint32_t)num_vectors, (uint64_t)max_vector_len) * sizeof(FF));
 }
 
 // Scratch bytes of phyloComparePairsMany for P pairs and at most max_tiles
 // merge tiles (sum over pairs of ceil((nl + nr) / phyloCompareTileElements())).
 long phyloComparePairsManyScratch(int num_pairs, long max_tiles) {
+    if (num_pairs < 0 || max_tiles < 0) return -1;
     return (long)compare_many_scratch_bytes((uint32_t)num_pairs, (uint64_t)max_tiles);
 }
 
@@ -669,6 +685,7 @@ int phyloComparePairsMany(uintptr_t stream, uintptr_t d_scratch, long scratch_si
                           uintptr_t d_lnnz, uintptr_t d_rkeys, uintptr_t d_rvalues,
                           uintptr_t d_roff, uintptr_t d_rnnz, uintptr_t d_pa, uintptr_t d_pb,
                           int num_pairs, long max_tiles, uintptr_t d_out) {
+    if (num_pairs < 0 || max_tiles < 0 || scratch_size < 0) return (int)cudaErrorInvalidValue;
     return (int)compare_many_launch(
         (cudaStream_t)stream, (void *)d_scratch, (size_t)scratch_size, (const uint32_t *)d_lkeys,
         (const float *)d_lvalues, (const uint64_t *)d_loff, (const uint32_t *)d_lnnz,
@@ -684,6 +701,7 @@ int phyloComparePairAsync(uintptr_t stream, uintptr_t d_scratch, long scratch_si
                           uintptr_t d_left_keys, uintptr_t d_left_values, int left_size,
                           uintptr_t d_right_keys, uintptr_t d_right_values, int right_size,
                           uintptr_t d_out) {
+    if (left_size < 0 || right_size < 0 || scratch_size < 0) return (int)cudaErrorInvalidValue;
     return (int)compare_launch((cudaStream_t)stream, (void *)d_scratch, (size_t)scratch_size,
                                (const uint32_t *)d_left_keys, (const float *)d_left_values,
                                (uint32_t)left_size, (const uint32_t *)d_right_keys,

@@ -127,3 +127,52 @@ def test_ctypes_declarations_match_the_header(lib):
         assert len(f.argtypes) == len(params), (name, len(f.argtypes), len(params))
         for i, (c_type, declared) in enumerate(zip(params, f.argtypes)):
             assert _ctype_ok(c_type, declared), (name, i, c_type, declared)
+
+
+def test_negative_sizes_refused_before_device_work(lib):
+    """Every entry point that takes a count or a byte size refuses a negative one
+    with cudaErrorInvalidValue before any device call (cast to an unsigned size it
+    would launch grids over memory the caller never passed).  No GPU here: a call
+    that got past its checks would return a CUDA error other than 1."""
+    INVALID = 1
+    P = b"protein"
+    buf = ctypes.create_string_buffer(256)
+    h = ctypes.addressof(buf)
+    z = [0] * 10
+    calls = {
+        "build scratch": lib.buildCompositionVector(0, 0, -1, P, 6, 0, 10, 0, 0, 0, 100),
+        "compare scratch": lib.compareCompositionVectors(0, 0, -1, 0, 0, 1, 0, 0, 1, 0),
+        "compare left": lib.compareCompositionVectors(0, 0, 100, 0, 0, -1, 0, 0, 1, 0),
+        "static right": lib.compareCompositionVectorsStatic(0, 0, 0, 1, 0, 0, -1, 0),
+        "plan cand": lib.phyloBuildBatchPlan(0, 0, 100, P, 6, 2, 0, 0, -1, h, h),
+        "plan scratch": lib.phyloBuildBatchPlan(0, 0, -1, P, 6, 2, 0, 0, 100, h, h),
+        "plan async": lib.phyloBuildBatchPlanAsync(0, 0, 100, P, 6, 2, 0, 0, -1, h),
+        "emit base": lib.phyloBuildBatchEmit(0, 0, 100, P, 6, 2, 100, 0, 0, 0, -5, 0),
+        "norms cand": lib.phyloBuildBatchNorms(0, 0, 100, P, 6, 2, -1, h),
+        "counts null": lib.phyloBuildBatchCounts(0, 0, 100, P, 6, 2, 100, 0, 0, 0, 0),
+        "window index n": lib.phyloWindowIndex(0, 0, 0, -1, 11, 10, 100, 0),
+        "window index len": lib.phyloWindowIndex(0, 0, 0, 4, 11, 10, -1, 0),
+        "pairs items": lib.phyloPairsLaunch(*([0] * 9), 10, 11, 0, 0, 0, -1, 0, 0, 28, 0,
+                                            16, 256, 152),
+        "pairs grid": lib.phyloPairsLaunch(*([0] * 9), 10, 11, 0, 0, 0, 4, 0, 0, 28, 0,
+                                           16, 256, 0),
+        "reduce tiles": lib.phyloPairsReduce(0, 0, 0, -1, 1, 16, 256, 0, 0, 0, 10, 1, 1),
+        "reduce segments": lib.phyloPairsReduce(0, 0, 0, 3, 0, 16, 256, 0, 0, 0, 10, 1, 1),
+        "reduce ldc": lib.phyloPairsReduce(0, 0, 0, 3, 4, 16, 256, 0, 0, 0, 0, 1, 1),
+        "self dot n": lib.phyloSelfDot(0, 0, 0, -1, 10, 0, 0, 10),
+        "self dot ldc": lib.phyloSelfDot(0, 0, 0, 4, 10, 0, 0, 0),
+        "many pairs": lib.phyloComparePairsMany(0, 0, 100, *z, -1, 10, 0),
+        "many tiles": lib.phyloComparePairsMany(0, 0, 100, *z, 4, -1, 0),
+        "pair async": lib.phyloComparePairAsync(0, 0, 100, 0, 0, -1, 0, 0, 1, 0),
+        "ranks len": lib.phyloKeyRanks(0, 0, 10 ** 12, 21 ** 6, 0, 0, 2, -1, 0, 0, 0),
+        "rank index len": lib.phyloKeyRankIndex(0, 0, 10 ** 12, 21 ** 6, 0, 0, 2, -1, 100, 0,
+                                                11, 10, 0, 0),
+        "postings items": lib.phyloPostingsLaunch(*([0] * 9), 10, 9, 0, 0, 0, -1,
+                                                  0, 0, 0, 0, 128, 152),
+        "postings tiles": lib.phyloPostingsReduce(0, 0, 0, -1, 128, 0, 0, 0, 10, 1, 1),
+    }
+    bad = {k: v for k, v in calls.items() if v != INVALID}
+    assert not bad, bad
+    assert lib.phyloSelfDotPartBytes(-1, 10) == -1 and lib.phyloSelfDotPartBytes(4, -1) == -1
+    assert lib.phyloComparePairsManyScratch(-1, 10) == -1
+    assert lib.phyloComparePairsManyScratch(4, -1) == -1
