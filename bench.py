@@ -602,7 +602,10 @@ def run_ours(args):
         del engine, arena, builder, out, flush, seq
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
-        line["serve"] = serve_run(args, short=True)
+        try:
+            line["serve"] = serve_run(args, short=True)
+        except Exception as e:  # the serving sub-run must not take the headline line with it
+            line["serve"] = {"metric": "serve latency per query batch", "error": repr(e)}
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
