@@ -589,7 +589,10 @@ def run_ours(args):
     }
     del graph
     if not args.no_plain:
-        line["plain"] = plain_path(arena, wl, seq, dev, n_pairs, N, peak, k=args.k)
+        try:
+            line["plain"] = plain_path(arena, wl, seq, dev, n_pairs, N, peak, k=args.k)
+        except Exception as e:  # an informative leg: recorded, the line is still printed
+            line["plain"] = {"error": repr(e)}
     if not args.no_cpu_baseline:
         cb = cpu_baseline(wl, n_pairs, N, seconds=args.ref_seconds, k=args.k)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample",
