@@ -1,9 +1,9 @@
 """bench.py's host side on the CPU: the reference arm's JSON line, the kernel names
 that key the ncu counter table, and the cost-model fit.  No GPU: the reference arm is
 the Java CPU path (the oracle's C port), timed on a small bounded sample here."""
-import argparse
 import json
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -16,14 +16,17 @@ import bench  # noqa: E402
 from rocket_gb300.engine import EngineConfig  # noqa: E402
 
 
-def test_reference_arm_line(monkeypatch, capsys):
-    monkeypatch.setenv("RANK", "0")
-    monkeypatch.setenv("WORLD_SIZE", "1")
-    args = argparse.Namespace(workload="cpu16", proteomes=4, k=6, steps=1, warmup=0,
-                              ref_seconds=0.2, gpus=1)
-    assert bench.run_reference(args) == 0
-    lines = [x for x in capsys.readouterr().out.splitlines() if x.startswith("{")]
-    assert len(lines) == 1
+def test_reference_arm_line():
+    """The reference arm as launched from the command line: exit 0 and exactly one
+    JSON line on stdout, with the contract's keys."""
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--workload", "cpu16", "--proteomes", "4", "--steps", "1",
+                        "--warmup", "0", "--ref-seconds", "0.2"],
+                       capture_output=True, text=True, env=env, cwd=ROOT, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.strip()]
+    assert len(lines) == 1 and lines[0].startswith("{"), r.stdout[-2000:]
     d = json.loads(lines[0])
     assert d["impl"] == "reference"
     assert d["metric"] == "pairwise CV distances/s" and d["unit"] == "pairs/s"
