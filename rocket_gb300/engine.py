@@ -192,14 +192,16 @@ class BatchBuilder:
         seq_off = np.asarray(seq_off, np.int64)
         n = len(seq_off) - 1
         lens = np.diff(seq_off)
-        if arena is None:
-            arena = self.new_arena(int(np.sum(8 * lens + 64)) + 1024, n)
-        if arena.vec_off.numel() < arena.n + n + 1:
-            arena.vec_off = _grow(arena.vec_off, arena.n + n + 1)
         s_obj = stream if stream is not None else torch.cuda.current_stream(self.device)
         if host is not None and (host.device.type != "cpu" or host.numel() < seq_off[-1]):
             raise ValueError("host residues: a CPU tensor covering seq_off")
         with torch.cuda.stream(s_obj):
+            # allocated on the stream the build runs on, so that freeing the arena is
+            # ordered after the work queued there
+            if arena is None:
+                arena = self.new_arena(int(np.sum(8 * lens + 64)) + 1024, n)
+            if arena.vec_off.numel() < arena.n + n + 1:
+                arena.vec_off = _grow(arena.vec_off, arena.n + n + 1)
             self._build_into(arena, seq, seq_off, lens, s_obj, host)
         return arena
 
