@@ -442,7 +442,13 @@ class PairEngine:
     def ensure_index(self, stream=None) -> None:
         """Builds (or extends to newly appended vectors) the window index; with
         ``compress``, first replaces the keys by their ranks in the union of the
-        arena's keys (recomputed for all vectors when vectors were appended)."""
+        arena's keys (recomputed for all vectors when vectors were appended).
+        Buffers are allocated, filled and read back on ``stream``, the stream the
+        index kernels run on."""
+        with torch.cuda.stream(stream):  # no-op for None: the current stream
+            self._ensure_index(stream)
+
+    def _ensure_index(self, stream) -> None:
         a = self.arena
         W = 1 << self.cfg.wshift
         st = _stream_handle(stream)
@@ -695,8 +701,8 @@ class PairEngine:
                              f"{self.cfg.algorithm}")
         s_obj = stream if stream is not None else torch.cuda.current_stream(self.device)
         st = int(s_obj.cuda_stream)
-        part = self._parts(plan)
-        with torch.cuda.stream(s_obj):
+        with torch.cuda.stream(s_obj):  # buffers on the stream the kernels use
+            part = self._parts(plan)
             self.counter.zero_()
         if events is not None:
             events[0].record(s_obj)
@@ -735,7 +741,9 @@ class PairEngine:
             maxlen = int(np.max(np.diff(a.off[:a.n + 1]))) if a.n else 1
             nb = int(self.L.phyloSelfDotPartBytes(a.n, maxlen))
             if self.self_part is None or self.self_part.numel() < nb:
-                self.self_part = torch.empty(max(nb, 8), dtype=torch.uint8, device=self.device)
+                with torch.cuda.stream(s_obj):
+                    self.self_part = torch.empty(max(nb, 8), dtype=torch.uint8,
+                                                 device=self.device)
             check(self.L.phyloSelfDot(st, _p(a.values), _p(a.vec_off), a.n, maxlen,
                                       _p(self.self_part), _p(out), plan.ldc))
             self.launches += 2
