@@ -145,7 +145,7 @@ def test_x_is_a_letter_and_y_is_19():
 
 # ---------------------------------------------------------------- formulations agree
 
-@pytest.mark.parametrize("k", [3, 4, 5])
+@pytest.mark.parametrize("k", [3, 4, 5, 6])
 def test_slot_loop_equals_candidates_protein(k):
     for seed in range(3):
         s = O.bindings_input(seed, 20000)
@@ -157,7 +157,7 @@ def test_slot_loop_equals_candidates_protein(k):
             assert np.array_equal(a[f], b[f])
 
 
-@pytest.mark.parametrize("k", [3, 5, 7, 9])
+@pytest.mark.parametrize("k", [3, 5, 7, 9, 10])
 def test_slot_loop_equals_candidates_dna(k):
     s = O.bindings_input(1, 20000, "DNA")
     a = O.cv_native(s, k, "DNA", formulation="slots", with_values=False)
