@@ -166,10 +166,11 @@ def test_slot_loop_equals_candidates_dna(k):
     assert np.array_equal(a["alpha"].view(np.uint32), b["alpha"].view(np.uint32))
 
 
-def test_count_tables_match_enumeration():
+@pytest.mark.parametrize("k", [4, 5, 6])
+def test_count_tables_match_enumeration(k):
     s = O.bindings_input(2, 30000)
-    k1, k2, tot = O.count_tables(s, 5)
-    r = O.cv_native(s, 5, with_values=False)
+    k1, k2, tot = O.count_tables(s, k)
+    r = O.cv_native(s, k, with_values=False)
     assert (r["n0"], r["n1"], r["n2"]) == tot
     assert tot[1] == int(k1.sum()) and tot[2] == int(k2.sum())
 
